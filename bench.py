@@ -1,0 +1,365 @@
+"""Benchmark of the GB300 position-based-fluids step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the 1,048,576-particle single scene): a 128 x 128 x 64 block of
+particles at spacing 0.05 (h = 0.1) in a 6.4 m cube with 64^3 cells, the
+paper equations (relaxation 600, s_corr k 0.1 n 4 dq 0.2 h, XSPH 0.01,
+vorticity 0.0005), 4 solver iterations, dt = 1/120, seeded jitter.  A step
+is one full simulation step (hash, sort, cell ranges, reorder, 4 x lambda
+and delta-p, vorticity, XSPH + commit).  The metric is particle-iterations/s
+= N particles x 4 solver iterations x steps / seconds.
+
+Our arm prints one JSON line with:
+  value     device-resident throughput: K steps replayed as CUDA graphs,
+            timed with CUDA events on the simulation's stream;
+  e2e       the same metric through the C-ABI with host buffers: every step
+            uploads the state from page-locked host memory, steps, and reads
+            the state back, all inside the timed region;
+  roofline  the dominant kernel's algorithmic bytes per launch over its
+            average launch time (a second timed pass with an event after
+            every launch), against the measured HBM copy bandwidth;
+  cpu_baseline  the reference's own kernels (compiled from their sources)
+            or, where they are absent, the oracle's restatement of them, on a
+            bounded sample of the same workload on the host cores.
+The working set (state, neighbour lists, sort buffers) is several hundred MB,
+larger than L2, so no flush runs between steps.
+
+--impl reference times the reference's own CPU implementation on the same
+workload and prints the same line with "impl": "reference".
+Under torchrun (N > 1) every rank runs an independent replica of the scene
+(replicas only: a single scene is not sharded); value sums all ranks' work
+over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+ITERATIONS = 4
+METRIC = "particle-iterations/s"
+UNIT = "particle-iterations/s"
+# Compulsory HBM bytes per particle and launch of each stage (neighbour
+# re-reads counted as cache hits): predict+hash 72, sort 52 (18-bit keys),
+# cell ranges 8, reorder 104, lambda 24, delta-p 36, vorticity 48,
+# XSPH+commit 84; 608 per particle-step in total.
+ALG_BYTES = {
+    "predict_hash": 72, "sort_onesweep": 52, "cell_offsets": 8, "reorder": 104,
+    "nbr_lambda": 24, "lambda": 24, "delta": 36, "vorticity": 48, "xsph_commit": 84,
+}
+STEP_BYTES = 608
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profile_traffic(kernel: str):
+    """dram read+write bytes per launch and particles per launch of `kernel`
+    from the committed ncu summary (profiles/*traffic*.txt lines of the form
+    `traffic kernel=<name> bytes_per_launch=<B> particles=<N>`), or None."""
+    for f in sorted((ROOT / "profiles").glob("*.txt")):
+        for line in f.read_text().splitlines():
+            if line.startswith("traffic ") and f"kernel={kernel} " in line + " ":
+                kv = dict(t.split("=", 1) for t in line.split()[1:] if "=" in t)
+                return float(kv["bytes_per_launch"]), float(kv["particles"])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu_index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = []
+        for line in Path(self.file.name).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ helpers
+def dist_info():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_group(world: int, backend: str):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def reduce_max(dist, value: float, device=None) -> float:
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_reference_run(n_steps_max: int = 10, budget_s: float = 15.0, threads: int = 0):
+    """Times the reference's own kernels (or the oracle restatement where
+    they are not built) on the 1M workload, one step at a time until
+    `budget_s` of CPU time is spent.  Returns (value, info)."""
+    import oracle
+    import __graft_entry__ as ge
+
+    pbf = ge.load_package()
+    sc = pbf.scenes.config_1m()
+    p = sc.params
+    cfg = oracle.Config(p.x_min, p.x_max, p.y_min, p.y_max, p.z_min, p.z_max, p.x_n, p.y_n, p.z_n,
+                        p.time_step_length, p.rest_density)
+    pos, vel = pbf.state_from_particles(sc.particles)
+    threads = threads or (os.cpu_count() or 1)
+    kind = "reference" if oracle.reference_available() else "port"
+    steps = 0
+    t0 = time.perf_counter()
+    while steps < n_steps_max:
+        if kind == "reference":
+            pos, vel, *_ = oracle.reference_steps(cfg, pos, vel, 1, threads=threads, parallel_cells=True)
+        else:
+            pos, vel, _, _ = oracle.refcompat_steps_f32(cfg, pos, vel, 1, threads=threads)
+        steps += 1
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    dt = time.perf_counter() - t0
+    value = sc.n * ITERATIONS * steps / dt
+    info = {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": f"{steps} step(s) of the {sc.n}-particle scene from its initial state, "
+                      f"reference equations, {'reference kernels compiled from their .cl sources' if kind == 'reference' else 'oracle restatement of the reference kernels'}, "
+                      f"{dt:.1f} s"}
+    return value, info
+
+
+# -------------------------------------------------------------------- arms
+def run_reference(args) -> int:
+    world, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    value, info = cpu_reference_run(n_steps_max=max(1, args.steps), budget_s=args.cpu_budget)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "single_scene_1m", "particles": 1048576, "cells": 262144,
+                   "solver_iterations": ITERATIONS, "equations": "reference kernels"},
+        "cpu_baseline": info,
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args) -> int:
+    import torch
+
+    import __graft_entry__ as ge
+
+    world, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    dist = make_group(world, "nccl")
+    pbf = ge.load_package()
+    sc = pbf.scenes.config_1m()
+    n = sc.n
+    sim = pbf.Simulation(sc.params, sc.particles)
+    sim.init()
+    sim.initCells()
+    ext = torch.cuda.ExternalStream(sim.stream())
+    launches = sim.launches_per_step()
+
+    # warm-up (also instantiates the step graph)
+    sim.step(args.warmup)
+
+    # ---- device-resident throughput ------------------------------------
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        e0.record(ext)
+        sim.step(args.steps, sync=False)
+        e1.record(ext)
+        e1.synchronize()
+    sim.sync()
+    t_dev = e0.elapsed_time(e1) / 1e3
+    t_dev = reduce_max(dist, t_dev, device="cuda")
+    value = world * n * ITERATIONS * args.steps / t_dev
+    clock_summary = clocks.summary()
+
+    # ---- end to end through the C-ABI with host buffers ------------------
+    nbytes = n * 16
+    hp = pbf.lib()
+    import ctypes as C
+
+    pin_pos, pin_vel = C.c_void_p(), C.c_void_p()
+    hp.pbf_host_alloc(nbytes, C.byref(pin_pos))
+    hp.pbf_host_alloc(nbytes, C.byref(pin_vel))
+    sim.dump_data_async(pin_pos.value, pin_vel.value)
+    sim.sync()
+    e2e_steps = max(3, min(args.steps, 20))
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(ext)
+    for _ in range(e2e_steps):
+        sim.set_state_async(pin_pos.value, pin_vel.value)
+        sim.step(1, sync=False)
+        sim.dump_data_async(pin_pos.value, pin_vel.value)
+    f1.record(ext)
+    f1.synchronize()
+    sim.sync()
+    t_e2e = reduce_max(dist, f0.elapsed_time(f1) / 1e3, device="cuda")
+    e2e_value = world * n * ITERATIONS * e2e_steps / t_e2e
+    final = np.frombuffer((C.c_float * (4 * n)).from_address(pin_pos.value), np.float32).reshape(n, 4)
+    finite = bool(np.isfinite(final).all())
+    hp.pbf_host_free(pin_pos)
+    hp.pbf_host_free(pin_vel)
+
+    # ---- per-kernel timing pass (events after every launch) -------------
+    sim.set_stage_timing(True)
+    kt_steps = max(3, min(args.steps, 10))
+    sim.step(kt_steps)
+    kt = sim.kernel_times()
+    stages = sim.stage_times()
+    sim.set_stage_timing(False)
+    total_ms = sum(ms for ms, _ in kt.values())
+    dom = max((k for k in kt if k in ALG_BYTES), key=lambda k: kt[k][0])
+    dom_ms, dom_launches = kt[dom]
+    per_launch_s = dom_ms / 1e3 / dom_launches
+    if dom == "sort_onesweep":
+        per_launch_s = dom_ms / 1e3 / kt_steps
+    peaks = measured_peaks()
+    achieved = ALG_BYTES[dom] * n / per_launch_s / 1e9
+    traffic = profile_traffic(dom)
+    roofline = {
+        "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+        "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+        "traffic": (traffic[0] * n / traffic[1]) if traffic else None,
+        "algorithmic_bytes_per_launch": ALG_BYTES[dom] * n,
+        "avg_launch_ms": per_launch_s * 1e3, "share_of_step": dom_ms / total_ms,
+    }
+    step_s = t_dev / args.steps
+    step_roofline = {"bytes_per_particle_step": STEP_BYTES,
+                     "achieved_gbs": STEP_BYTES * n / step_s / 1e9,
+                     "frac": STEP_BYTES * n / step_s / 1e9 / peaks["hbm_gbs"]}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        _, cpu = cpu_reference_run(budget_s=args.cpu_budget)
+
+    sim.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "single_scene_1m", "particles": n, "cells": sc.params.ncells,
+                       "box": [6.4, 6.4, 6.4], "block": [128, 128, 64], "solver_iterations": ITERATIONS,
+                       "equations": "paper (relaxation 600, s_corr, XSPH, vorticity)",
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "working set larger than L2; no flush between steps",
+                       "graph": True},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
+                    "d2h_bytes_per_step": 2 * nbytes, "steps": e2e_steps, "finite": finite},
+            "gpu_launches": launches * args.steps,
+            "roofline": roofline,
+            "step_roofline": step_roofline,
+            "stage_ms": {"sort": float(stages[0]), "lambda": float(stages[1]), "delta_p": float(stages[2]),
+                         "velocity": float(stages[3])},
+            "kernel_ms_per_step": {k: v[0] / kt_steps for k, v in kt.items()},
+            "clocks": clock_summary,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline work")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

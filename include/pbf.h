@@ -1,0 +1,254 @@
+/*
+ * pbf.h -- C-ABI of the GB300 position-based-fluids (PBF) step.
+ *
+ * This is the drop-in boundary for the simulation step of
+ * MrMagne/position-based-fluids.  It replaces two reference interfaces:
+ *
+ *  1. the Simulation step interface (src/Simulation.hpp:41-108): construct,
+ *     init(), initCells(), step(), dumpData(), the size getters and
+ *     setWaveGenerator(); the reference's caller is Runner::run
+ *     (src/Runner.cpp:43-46,83,102);
+ *  2. the kernel operator interface for the neighbour structure, i.e. the
+ *     `__kernel` entry points the reference looks up by name
+ *     (src/ocl/clsetup.cpp:343-358) for the cell hash (update_cells.cl,
+ *     calc_hash.cl), the radix sort of (cell, particle) keys
+ *     (radix_histogram.cl, radix_scan.cl, radix_paste.cl, radix_reorder.cl)
+ *     and the cell ranges (init_cells.cl, find_cells.cl).
+ *
+ * Conventions
+ *  - Every function returns an int status (pbf_status); no exception crosses
+ *    the boundary.  The reference throws cl::Error / std::runtime_error
+ *    (src/hesp.hpp:33, src/io/*.cpp) and its main() exits on them
+ *    (src/main.cpp:180-186).
+ *  - Host arrays of particle state use the reference's dumpData layout
+ *    (src/Simulation.cpp:578-591, 120-134): N float4 positions with
+ *    .w = |v| after a step (0 before the first step), N float4 velocities
+ *    with .w = particle mass.
+ *  - A pbf_sim owns one CUDA stream.  Calls on one pbf_sim are not
+ *    thread-safe; separate pbf_sim objects are independent.  pbf_step is
+ *    asynchronous; pbf_sync, pbf_dump_data and the getters that read device
+ *    state synchronise.
+ *  - `void *stream` arguments are cudaStream_t values (0 = legacy default).
+ *  - Device-pointer arguments (d_*) point to memory of the current CUDA
+ *    device.
+ */
+#ifndef PBF_GB300_H
+#define PBF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBF_ABI_VERSION 1
+
+typedef enum {
+  PBF_OK = 0,
+  PBF_ERR_INVALID = 1,  /* bad argument or parameter combination          */
+  PBF_ERR_OOM = 2,      /* device or pinned-host allocation failed         */
+  PBF_ERR_CUDA = 3,     /* CUDA runtime error (see pbf_last_error_message) */
+  PBF_ERR_DEVICE = 4,   /* a kernel's bounded wait gave up; results void   */
+  PBF_ERR_IO = 5,       /* file could not be opened or parsed              */
+  PBF_ERR_BUDGET = 6,   /* request does not fit the HBM budget             */
+  PBF_ERR_STATE = 7,    /* call out of order (e.g. step before init)       */
+  PBF_ERR_NOT_FOUND = 8 /* unknown scene / request id                      */
+} pbf_status;
+
+/* Equation set of the solver. */
+typedef enum {
+  /* The reference's kernels as shipped: relaxation 1e4, no s_corr, no
+   * vorticity, density without the self term, XSPH c = 0.01 with 1/rho_j,
+   * walls at h from the box, constants rounded to 6 significant digits as
+   * src/main.cpp:149-168 prints them.  Results match the reference's
+   * kernels run with each cell list in descending particle order. */
+  PBF_MODE_REF_COMPAT = 0,
+  /* Macklin & Mueller 2013 with the relaxation epsilon, s_corr, XSPH and
+   * vorticity confinement taken from pbf_params; neighbour sets fixed at
+   * the start of each step. */
+  PBF_MODE_PAPER = 1
+} pbf_mode;
+
+/* ConfigParameters (src/Parameters.hpp:12-31) followed by the solver
+ * settings the reference hard-codes in its kernels.  pbf_params_default
+ * fills every field; pbf_read_config overwrites the fields a .par file
+ * names (src/io/ConfigReader.cpp:45-84 keys, plus the extension keys listed
+ * beside each field). */
+typedef struct {
+  char part_input_file[256];      /* part_input_file                      */
+  float time_step_length;         /* timestep_length                      */
+  float time_end;                 /* time_end                             */
+  uint32_t part_out_freq;         /* part_out_freq                        */
+  char part_out_name_base[256];   /* part_out_name_base                   */
+  uint32_t vtk_out_freq;          /* vtk_out_freq                         */
+  char vtk_out_name_base[256];    /* vtk_out_name_base                    */
+  uint32_t cl_workgroup_1dsize;   /* cl_workgroup_1dsize (unused)         */
+  float x_min, x_max, y_min, y_max, z_min, z_max; /* x_min ... z_max      */
+  float x_n, y_n, z_n;            /* x_n y_n z_n: cells per axis          */
+  float rest_density;             /* restdensity: particles per volume    */
+  /* ---- extensions (keys in brackets) ---- */
+  int32_t mode;                   /* [mode] ref_compat | paper            */
+  uint32_t solver_iterations;     /* [solver_iterations] reference: 4     */
+  float relax_eps;                /* [relax_eps] paper mode               */
+  float scorr_k;                  /* [scorr_k]                            */
+  float scorr_dq;                 /* [scorr_dq] fraction of h             */
+  int32_t scorr_n;                /* [scorr_n]                            */
+  float xsph_c;                   /* [xsph_c]                             */
+  float vort_eps;                 /* [vort_eps]                           */
+  float gravity_y;                /* [gravity_y] paper mode               */
+  float wall_margin;              /* [wall_margin] paper mode, in metres  */
+  uint32_t max_neighbours;        /* [max_neighbours] stored per particle */
+} pbf_params;
+
+/* Particle (src/Particle.hpp:9-14): mass, position, velocity, acceleration
+ * (the acceleration is never read, as in the reference). */
+typedef struct {
+  float m;
+  float x[3];
+  float v[3];
+  float a[3];
+} pbf_particle;
+
+/* ------------------------------------------------------------------ misc */
+int pbf_abi_version(void);
+const char *pbf_status_string(int status);
+/* Text of the last CUDA error seen by this thread (empty if none). */
+const char *pbf_last_error_message(void);
+
+/* Defaults: mode PAPER, 4 iterations, relax_eps 600, s_corr k 0.1 n 4
+ * dq 0.2, XSPH c 0.01, vorticity eps 0.0005, gravity -9.81, wall margin
+ * h/4 (resolved at create time when negative), max_neighbours 64. */
+void pbf_params_default(pbf_params *p);
+
+/* ------------------------------------------------ scenario layer (L0) */
+/* ConfigReader::read (src/io/ConfigReader.cpp:19-91).  Fields absent from
+ * the file keep the values already in *out (call pbf_params_default
+ * first); unknown keys are skipped with a warning on stderr, as in the
+ * reference. */
+int pbf_read_config(const char *path, pbf_params *out);
+/* PartReader::read (src/io/PartReader.cpp:21-95): first line N, then one
+ * "m x y z vx vy vz" line per particle.  *out is allocated by the library
+ * (release with pbf_free); a malformed line ends the read with the
+ * particles parsed so far and a warning, as in the reference. */
+int pbf_read_particles(const char *path, pbf_particle **out, uint32_t *n);
+void pbf_free(void *ptr);
+/* DataLoader::getPathFor* (src/DataLoader.cpp:20-31) with an explicit root
+ * instead of the executable's directory: root/data/<kind>s/<name> for kind
+ * "scenario", "kernel", "shader" or "texture". */
+int pbf_data_path(const char *root, const char *kind, const char *name,
+                  char *out, size_t cap);
+/* Lattice block generator (the semantics of tools/gen_grid.py, with seeded
+ * jitter): nx*ny*nz particles at `spacing` from `origin`, each coordinate
+ * jittered by U(-jitter, +jitter) from a splitmix64 stream seeded with
+ * `seed`, zero velocity, mass `mass`.  `out` holds nx*ny*nz particles. */
+int pbf_generate_block(const float origin[3], uint32_t nx, uint32_t ny,
+                       uint32_t nz, float spacing, float jitter, float mass,
+                       uint64_t seed, pbf_particle *out);
+
+/* ---------------------------------------- Simulation step interface (L3) */
+typedef struct pbf_sim pbf_sim;
+
+/* Simulation::Simulation.  Copies the parameters and particles; no device
+ * work yet.  Rejects: n == 0, a grid with fewer than one cell per axis or
+ * more than 2^31 cells, a non-positive time step or rest density, and in
+ * paper mode a cell shorter than h on any axis (the 27-cell search would
+ * miss neighbours). */
+int pbf_create(const pbf_params *params, const pbf_particle *particles,
+               uint32_t n, pbf_sim **out);
+/* Simulation::init: selects the current CUDA device, creates the stream,
+ * allocates device state and uploads the particles. */
+int pbf_init(pbf_sim *sim);
+/* Simulation::initCells: validates that init ran.  The neighbour structure
+ * is rebuilt inside every step, so there is no separate cell state. */
+int pbf_init_cells(pbf_sim *sim);
+/* Simulation::step, `nsteps` times, enqueued on the sim's stream. */
+int pbf_step(pbf_sim *sim, uint32_t nsteps);
+/* Waits for the sim's stream; returns PBF_ERR_DEVICE if a kernel reported
+ * an error since the last check. */
+int pbf_sync(pbf_sim *sim);
+/* Simulation::dumpData into caller memory: pos4/vel4 hold N float4 each,
+ * in the input particle order.  Blocking. */
+int pbf_dump_data(pbf_sim *sim, float *pos4, float *vel4);
+/* Replaces the state (same layout as pbf_dump_data).  Blocking. */
+int pbf_set_state(pbf_sim *sim, const float *pos4, const float *vel4);
+/* Stream-ordered variants for page-locked host buffers: they return after
+ * enqueueing; the copies complete in stream order. */
+int pbf_set_state_async(pbf_sim *sim, const float *pos4, const float *vel4);
+int pbf_dump_data_async(pbf_sim *sim, float *pos4, float *vel4);
+/* Page-locked host buffer helpers for the async variants. */
+int pbf_host_alloc(size_t bytes, void **out);
+int pbf_host_free(void *ptr);
+/* Simulation::setWaveGenerator: offset of the moving x-min wall. */
+int pbf_set_wave(pbf_sim *sim, float value);
+int pbf_get_num_particles(const pbf_sim *sim, uint32_t *n);
+/* getSizesMin / getSizesMax (.w = 0). */
+int pbf_get_sizes(const pbf_sim *sim, float min4[4], float max4[4]);
+/* The cudaStream_t of the sim (valid after pbf_init). */
+int pbf_get_stream(const pbf_sim *sim, void **stream);
+/* Per-stage device times of the last step run with timing enabled:
+ * ms[0] neighbour search (predict, hash, sort, cell ranges, reorder),
+ * ms[1] lambda passes, ms[2] delta-p passes, ms[3] velocity update.
+ * Enabling timing turns off CUDA-graph replay for the timed steps. */
+int pbf_set_stage_timing(pbf_sim *sim, int enable);
+int pbf_stage_times(pbf_sim *sim, float ms[4]);
+/* Per-kernel device times accumulated over every step run since timing was
+ * last enabled: for entry q < min(cap, *count), names[32q..32q+31] is the
+ * kernel (or kernel group) name, total_ms[q] its summed time and
+ * launches[q] its number of kernel launches.  *count receives the number of
+ * entries; any output pointer but count may be NULL. */
+int pbf_kernel_times(pbf_sim *sim, uint32_t cap, char *names, float *total_ms,
+                     uint32_t *launches, uint32_t *count);
+/* Replays each step as one CUDA graph (default on). */
+int pbf_set_graph(pbf_sim *sim, int enable);
+/* Number of this library's kernel launches one step issues. */
+int pbf_launches_per_step(const pbf_sim *sim, uint32_t *launches);
+/* Density of every particle from the last lambda pass of the last step
+ * (input order). */
+int pbf_get_density(pbf_sim *sim, float *density);
+/* The neighbour structure the last step built, in input particle order:
+ * hash[i] = cell of particle i; perm[q] = input index of the particle at
+ * sorted position q (ties by input index in REF_COMPAT mode, by previous
+ * sorted position in PAPER mode); ranges = inclusive (first,last) int2 per
+ * cell, (-1,-1) if empty.  Any pointer may be NULL. */
+int pbf_get_cells(pbf_sim *sim, uint32_t *hash, uint32_t *perm,
+                  int32_t *ranges);
+int pbf_destroy(pbf_sim *sim);
+
+/* ------------------------------------ neighbour-structure operators (L4) */
+/* Cell hash of N predicted positions (float4, .w ignored) on the grid of
+ * `params` (update_cells.cl:10-15 / calc_hash.cl:15-20).  Each axis cell
+ * is trunc((p - min) / cell_length) clamped to [0, n-1]; inside the grid
+ * the clamp never fires. */
+int pbf_op_cell_hash(const pbf_params *params, const float *d_pred4,
+                     uint32_t n, uint32_t *d_hash, void *stream);
+/* Bytes of device scratch pbf_op_sort_pairs needs. */
+size_t pbf_op_sort_scratch_bytes(uint32_t n, uint32_t key_bits);
+/* Stable LSD radix sort of (key, value) pairs by the low `key_bits` bits
+ * of key (onesweep: one histogram pass, then one pass per 8-bit digit with
+ * decoupled look-back).  d_vals_in may be NULL, meaning values 0..n-1,
+ * which makes d_vals_out the stable permutation (ties by index).  Inputs
+ * are not modified; outputs must not alias inputs.  Keys must be < 2^key_bits. */
+int pbf_op_sort_pairs(const uint32_t *d_keys_in, const uint32_t *d_vals_in,
+                      uint32_t n, uint32_t key_bits, uint32_t *d_keys_out,
+                      uint32_t *d_vals_out, void *d_scratch,
+                      size_t scratch_bytes, void *stream);
+/* Synchronises `stream` and reports PBF_ERR_DEVICE if the last
+ * pbf_op_sort_pairs with this scratch, n and key_bits had a look-back wait
+ * give up (its output is then void). */
+int pbf_op_sort_status(const void *d_scratch, uint32_t n, uint32_t key_bits,
+                       void *stream);
+/* CSR cell offsets of sorted keys: d_offsets[c] = number of keys < c for
+ * c in [0, ncells]; every key must be < ncells. */
+int pbf_op_cell_offsets(const uint32_t *d_sorted_keys, uint32_t n,
+                        uint32_t ncells, uint32_t *d_offsets, void *stream);
+/* The reference's cell ranges (init_cells.cl + find_cells.cl intent):
+ * inclusive (first,last) int2 per cell, (-1,-1) if empty. */
+int pbf_op_find_cells(const uint32_t *d_offsets, uint32_t ncells,
+                      int32_t *d_first_last, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PBF_GB300_H */

@@ -355,7 +355,11 @@ int refcompat_steps(const oracle_config *cfg, uint32_t n, T *pos4, T *vel4,
  *   lambda_i  = -(rho_i/rho0 - 1) / ((|sum_j g_ij|^2 + sum_j |g_ij|^2)/rho0^2
  *                                     + eps)
  *   dp_i      = (1/rho0) sum_j (lambda_i + lambda_j + s_corr_ij) g_ij,
- *   s_corr_ij = -k (W_poly6(r_ij) / W_poly6(dq h))^n
+ *   s_corr_ij = -k h^2 (W_poly6(r_ij) / W_poly6(dq h))^n
+ *               (s_corr is added to lambda, which has units of area; the
+ *               paper's dimensionless k is taken in units of h^2.  Read as
+ *               k m^2 at h = 0.1 m it outweighs lambda a thousandfold and a
+ *               resting block flies apart within 20 steps.)
  *   collision = clamp to [min + margin (+wave on x-min), max - margin]
  *   v_i       = (p_i - x_i) / dt
  *   omega_i   = sum_j (1/rho_j) g_ij x (v_j - v_i)
@@ -486,7 +490,7 @@ struct Paper {
         double g[3], r2;
         if (!grad(i, j, g, &r2)) continue;
         const double ratio = std::pow((h2 - r2) / dn, 3.0 * sn);
-        const double sc = -prm.scorr_k * ratio;
+        const double sc = -prm.scorr_k * h2 * ratio;
         const double w = lam[i] + lam[j] + sc;
         s[0] += w * g[0];
         s[1] += w * g[1];

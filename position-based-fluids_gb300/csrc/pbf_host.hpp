@@ -1,0 +1,34 @@
+// Host-side helpers shared by the C-ABI translation units (no device code).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/pbf.h"
+#include "pbf_internal.cuh"
+
+namespace pbf {
+
+// Records the text of a CUDA error for pbf_last_error_message and maps it to
+// a status code.
+int cuda_status(cudaError_t e, const char *where);
+void set_error_message(const std::string &msg);
+
+// The reference's constant baking (src/main.cpp:149-168): a value printed
+// with std::showpoint at precision 6 and read back as a float literal.
+float baked6(double v);
+
+// Derived constants.  `h` is (x_max - x_min) / x_n in float arithmetic, as
+// src/main.cpp:164 computes it.
+float params_h(const pbf_params &p);
+RefConsts make_ref_consts(const pbf_params &p);
+PaperConsts make_paper_consts(const pbf_params &p, uint32_t n);
+// Scene descriptor of the whole box of `p` (grid origin, cell lengths,
+// clamp bounds).  cell_base / particle range are left for the caller.
+SceneDesc make_scene(const pbf_params &p);
+// Validates a parameter set for a simulation of n particles.
+int validate_params(const pbf_params &p, uint32_t n);
+uint64_t grid_cells(const pbf_params &p);
+
+}  // namespace pbf

@@ -1,0 +1,185 @@
+// Internal declarations shared by the CUDA translation units of the GB300
+// position-based-fluids library.  Nothing here crosses the C-ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstddef>
+
+namespace pbf {
+
+// ---------------------------------------------------------------- errors --
+// Device-side error bits, OR-ed into a per-simulation flag word that the
+// host reads back at synchronisation points.
+enum DeviceError : uint32_t {
+  kDevErrLookback = 1u,  // a radix-sort look-back wait hit its bound
+};
+
+// ------------------------------------------------------------ grid / scene --
+// One simulation box with its uniform cell grid.  In the single-scene path
+// the table has one entry; a batch holds one entry per scene, each owning
+// the key range [cell_base, cell_base + ncell.x*ncell.y*ncell.z) and the
+// particle range [p_begin, p_end) of the sorted state.
+struct SceneDesc {
+  float gmin[3];      // grid origin (the box minimum)
+  float clen[3];      // cell lengths
+  int32_t ncell[3];   // cells per axis
+  uint32_t cell_base; // first key of this scene
+  float lo[3];        // lowest admissible position per axis (x without wave)
+  float hi[3];        // highest admissible position per axis
+  float wave;         // moving x-min wall offset
+  uint32_t p_begin;   // first particle (sorted state)
+  uint32_t p_end;     // one past the last particle
+  uint32_t pad_;
+};
+
+// Solver constants of the paper equations (PBF_MODE_PAPER).
+struct PaperConsts {
+  float dt, gy;
+  float h, h2, poly6, spiky, w_self;
+  float rho0, inv_rho0, relax_eps;
+  float scorr_k, inv_scorr_den;  // 1 / (h^2 - (dq h)^2)
+  int32_t scorr_n3;              // 3 * n
+  float xsph_c, vort_eps;
+  uint32_t n, maxn;
+};
+
+// The 18 constants the reference bakes into its OpenCL program
+// (src/main.cpp:149-168), already rounded to 6 significant digits.
+struct RefConsts {
+  float min[3], max[3];
+  float ncell[3];
+  float clen[3];
+  float dt, rest_density, h, h2, poly6, spiky;
+  uint32_t n;  // particles
+};
+
+// ------------------------------------------------------------------ sort --
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;
+constexpr int kMaxSortPasses = 4;
+
+// Layout of the radix-sort scratch inside one allocation (32-bit words).
+struct SortPlan {
+  uint32_t n = 0, key_bits = 0, passes = 0, tiles = 0;
+  size_t off_hist = 0;      // passes * kRadix: digit histograms, then prefixes
+  size_t off_counter = 0;   // 32 words: per-pass tile counters
+  size_t off_lookback = 0;  // passes * tiles * kRadix
+  size_t clear_words = 0;   // words from off_hist that must start at zero
+  size_t off_keys_alt = 0;  // n
+  size_t off_vals_alt = 0;  // n
+  size_t words = 0;         // total
+};
+
+SortPlan make_sort_plan(uint32_t n, uint32_t key_bits);
+uint32_t bits_for(uint32_t max_key_exclusive);
+
+// Zeroes the histogram/counter/look-back words of `scratch`.
+cudaError_t sort_clear(const SortPlan &plan, uint32_t *scratch,
+                       cudaStream_t stream);
+// Digit histograms of keys (all passes); expects sort_clear first.
+cudaError_t sort_histogram(const SortPlan &plan, const uint32_t *keys,
+                           uint32_t *scratch, cudaStream_t stream);
+// Exclusive prefix of each pass histogram, in place.
+cudaError_t sort_scan(const SortPlan &plan, uint32_t *scratch,
+                      cudaStream_t stream);
+// The digit passes (histograms must be scanned).  vals_in may be null
+// (values = index).  Results land in keys_out / vals_out; inputs are left
+// untouched.
+cudaError_t sort_passes(const SortPlan &plan, const uint32_t *keys_in,
+                        const uint32_t *vals_in, uint32_t *keys_out,
+                        uint32_t *vals_out, uint32_t *scratch, uint32_t *err,
+                        cudaStream_t stream);
+cudaError_t cell_offsets(const uint32_t *sorted_keys, uint32_t n,
+                         uint32_t ncells, uint32_t *offsets,
+                         cudaStream_t stream);
+cudaError_t find_cells(const uint32_t *offsets, uint32_t ncells,
+                       int32_t *first_last, cudaStream_t stream);
+cudaError_t cell_hash(const float4 *pred, uint32_t n, const SceneDesc &scene,
+                      uint32_t *hash, cudaStream_t stream);
+// Number of kernel launches of one sort (histogram not included).
+uint32_t sort_pass_launches(const SortPlan &plan);
+
+// --------------------------------------------------------- device buffers --
+// Everything one plain (single-scene) simulation keeps on the device.
+struct DeviceState {
+  // persistent particle state
+  float4 *X = nullptr, *V = nullptr;   // positions (.w=|v|), velocities (.w=m)
+  uint32_t *ID = nullptr;              // input index of each slot (paper)
+  // step scratch
+  float4 *X2 = nullptr, *V2 = nullptr; // reordered state (paper)
+  uint32_t *ID2 = nullptr;
+  float4 *P = nullptr, *Q = nullptr;   // predicted positions (+lambda)
+  float4 *D = nullptr;                 // displacement since step start (paper)
+  float4 *U = nullptr;                 // velocity and 1/rho (paper)
+  float4 *W = nullptr;                 // vorticity and |omega| (paper)
+  float4 *P2 = nullptr, *DV = nullptr; // ref-compat ping-pong and dv
+  float *R = nullptr;                  // density
+  float *S = nullptr;                  // lambda (ref-compat)
+  uint32_t *keys = nullptr, *skeys = nullptr, *perm = nullptr;
+  uint32_t *offsets = nullptr;         // ncells + 1
+  uint32_t *nbr = nullptr, *nbr_cnt = nullptr; // neighbour lists (paper)
+  uint32_t *sort_scratch = nullptr;
+  uint32_t *err = nullptr;             // device error flag word
+  SceneDesc *scenes = nullptr;         // device scene table (1 entry)
+  float4 *io_pos = nullptr, *io_vel = nullptr; // input-order staging
+};
+
+// ------------------------------------------------------- paper-mode launches
+cudaError_t paper_predict_hash(const float4 *X, const float4 *V, uint32_t n,
+                               const PaperConsts &c, const SceneDesc *scenes,
+                               const uint16_t *sid, uint32_t *keys,
+                               const SortPlan &plan, uint32_t *sort_scratch,
+                               cudaStream_t st);
+cudaError_t paper_reorder(const uint32_t *perm, const float4 *X,
+                          const float4 *V, const uint32_t *ID, uint32_t n,
+                          const PaperConsts &c, float4 *X2, float4 *V2,
+                          uint32_t *ID2, float4 *P, float4 *D, cudaStream_t st);
+cudaError_t paper_nbr_lambda(const DeviceState &d, const PaperConsts &c,
+                             const uint16_t *sid, cudaStream_t st);
+cudaError_t paper_lambda(const DeviceState &d, const PaperConsts &c,
+                         const uint16_t *sid, cudaStream_t st);
+cudaError_t paper_delta(const DeviceState &d, const PaperConsts &c,
+                        const uint16_t *sid, bool last, cudaStream_t st);
+cudaError_t paper_vorticity(const DeviceState &d, const PaperConsts &c,
+                            const uint16_t *sid, cudaStream_t st);
+cudaError_t paper_xsph_commit(const DeviceState &d, const PaperConsts &c,
+                              const uint16_t *sid, cudaStream_t st);
+// state <-> input order
+cudaError_t gather_to_input_order(const float4 *X, const float4 *V,
+                                  const uint32_t *ID, uint32_t n,
+                                  float4 *out_pos, float4 *out_vel,
+                                  cudaStream_t st);
+cudaError_t scatter_from_input_order(const float4 *in_pos,
+                                     const float4 *in_vel, const uint32_t *ID,
+                                     uint32_t n, float4 *X, float4 *V,
+                                     cudaStream_t st);
+cudaError_t gather_scalar_to_input_order(const float *src, const uint32_t *ID,
+                                         uint32_t n, float *out,
+                                         cudaStream_t st);
+cudaError_t iota_u32(uint32_t *dst, uint32_t n, cudaStream_t st);
+
+// --------------------------------------------------- ref-compat launches --
+cudaError_t rc_predict_hash(float4 *X, float4 *V, float4 *P, uint32_t n,
+                            const RefConsts &k, const SceneDesc *scenes,
+                            uint32_t *keys, const SortPlan &plan,
+                            uint32_t *sort_scratch, cudaStream_t st);
+cudaError_t rc_lambda(float4 *P, float *S, const uint32_t *perm,
+                      const uint32_t *offsets, uint32_t n, const RefConsts &k,
+                      cudaStream_t st);
+cudaError_t rc_delta(const float4 *P, float4 *P2, const float *S,
+                     const uint32_t *perm, const uint32_t *offsets,
+                     const float4 *X, float4 *V, uint32_t n,
+                     const RefConsts &k, const SceneDesc *scenes, bool last,
+                     cudaStream_t st);
+cudaError_t rc_xsph(const float4 *P, const float4 *V, float4 *DV,
+                    const uint32_t *perm, const uint32_t *offsets, uint32_t n,
+                    const RefConsts &k, cudaStream_t st);
+cudaError_t rc_commit(float4 *X, float4 *V, const float4 *P, const float4 *DV,
+                      uint32_t n, cudaStream_t st);
+
+}  // namespace pbf

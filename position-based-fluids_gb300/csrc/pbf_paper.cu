@@ -1,0 +1,511 @@
+// Solver kernels of the GB300 position-based-fluids step, paper equations
+// (PBF_MODE_PAPER): Macklin & Mueller, "Position Based Fluids", ACM TOG
+// 32(4) 2013, Algorithm 1.  The reference's kernels this path replaces:
+//   predict_positions.cl, update_cells.cl / calc_hash.cl (predict + hash),
+//   compute_scaling.cl (lambda), compute_delta.cl + update_predicted.cl
+//   (delta p with s_corr, wall clamp, Jacobi apply), update_velocities.cl,
+//   apply_vorticity_and_viscosity.cl + update_positions.cl (vorticity
+//   confinement, XSPH, commit).
+//
+// Layout: the particle state stays sorted by cell from one step to the next
+// (X, V, and ID = input index), so the reorder gather after each sort reads
+// nearly sequential memory.  After the sort every array below is indexed by
+// sorted slot k:
+//   X2, V2  state at the start of the step, V2 with gravity applied
+//   P       predicted position x + d
+//   D       displacement d since the start of the step (kept apart from x so
+//           that positions round once per step, not once per iteration)
+//   Q       (predicted position, lambda) as read by the delta-p pass
+//   U       (velocity, 1/rho) as read by the velocity passes
+//   W       (vorticity, |vorticity|)
+//   nbr     neighbour lists, slot-major: nbr[s*N + k]
+// Neighbour sets are built once per step from the predicted positions
+// (Algorithm 1 line 6): N_k = { j != k : 0 < |p_k - p_j| < h } over the 27
+// cells around k's cell.  Every later pass evaluates the kernels at the
+// current positions with W = 0 beyond h.  A particle whose set exceeds the
+// list capacity keeps the true count, and every pass re-derives its set
+// from the cells and the step-start positions instead of the list.
+#include "pbf_device.cuh"
+
+namespace pbf {
+
+namespace {
+
+constexpr int kGatherThreads = 128;
+
+struct NbrCtx {
+  const uint32_t *__restrict__ nbr;
+  const uint32_t *__restrict__ cnt;
+  const uint32_t *__restrict__ skeys;
+  const uint32_t *__restrict__ off;
+  const float4 *__restrict__ X2;
+  const float4 *__restrict__ V2;
+  const SceneDesc *__restrict__ scenes;
+  const uint16_t *__restrict__ sid;
+  uint32_t n, maxn;
+  float dt, h2;
+};
+
+__device__ __forceinline__ const SceneDesc &scene_of(const SceneDesc *scenes,
+                                                     const uint16_t *sid,
+                                                     uint32_t k) {
+  return scenes[sid ? sid[k] : 0];
+}
+
+// v' = v + dt g;  d = dt v';  p = x + d  -- rounded op by op (no
+// contraction) so that every kernel that recomputes them gets the same bits.
+__device__ __forceinline__ float4 gravity_velocity(float4 v, float dt,
+                                                   float gy) {
+  v.y = __fadd_rn(v.y, __fmul_rn(dt, gy));
+  return v;
+}
+__device__ __forceinline__ float3 displacement(float4 v1, float dt) {
+  return make_float3(__fmul_rn(dt, v1.x), __fmul_rn(dt, v1.y),
+                     __fmul_rn(dt, v1.z));
+}
+__device__ __forceinline__ float3 add3(float4 x, float3 d) {
+  return make_float3(__fadd_rn(x.x, d.x), __fadd_rn(x.y, d.y),
+                     __fadd_rn(x.z, d.z));
+}
+
+// Step-start predicted position of slot j (as written by the reorder).
+__device__ __forceinline__ float3 start_position(const NbrCtx &c, uint32_t j) {
+  return add3(__ldg(&c.X2[j]), displacement(__ldg(&c.V2[j]), c.dt));
+}
+
+// Visits the particles of the 27 cells around the cell with key `key`, in
+// the order (dz, dy, sorted slot), skipping k itself.
+template <typename F>
+__device__ __forceinline__ void scan_cells(uint32_t k, uint32_t key,
+                                           const SceneDesc &s,
+                                           const uint32_t *__restrict__ off,
+                                           F &&f) {
+  const int nx = s.ncell[0], ny = s.ncell[1], nz = s.ncell[2];
+  const uint32_t local = key - s.cell_base;
+  const int cx = (int)(local % (uint32_t)nx);
+  const uint32_t t = local / (uint32_t)nx;
+  const int cy = (int)(t % (uint32_t)ny);
+  const int cz = (int)(t / (uint32_t)ny);
+  const int x0 = cx > 0 ? cx - 1 : 0;
+  const int x1 = cx + 1 < nx ? cx + 1 : nx - 1;
+  for (int dz = -1; dz <= 1; ++dz) {
+    const int z = cz + dz;
+    if (z < 0 || z >= nz) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = cy + dy;
+      if (y < 0 || y >= ny) continue;
+      const uint32_t row =
+          s.cell_base + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+      const uint32_t a = __ldg(&off[row + x0]);
+      const uint32_t b = __ldg(&off[row + x1 + 1]);
+      for (uint32_t j = a; j < b; ++j)
+        if (j != k) f(j);
+    }
+  }
+}
+
+// Visits N_k: from the list, or (list overflow) from the cells with the
+// membership test at the step-start positions, in the same order.
+template <typename F>
+__device__ __forceinline__ void visit_neighbours(const NbrCtx &c, uint32_t k,
+                                                 uint32_t count, F &&f) {
+  if (count <= c.maxn) {
+    for (uint32_t s = 0; s < count; ++s) f(__ldg(&c.nbr[(size_t)s * c.n + k]));
+  } else {
+    const SceneDesc &sc = scene_of(c.scenes, c.sid, k);
+    const float3 pk = start_position(c, k);
+    scan_cells(k, __ldg(&c.skeys[k]), sc, c.off, [&](uint32_t j) {
+      const float3 pj = start_position(c, j);
+      const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
+      const float r2 = rx * rx + ry * ry + rz * rz;
+      if (r2 > 0.0f && r2 < c.h2) f(j);
+    });
+  }
+}
+
+__device__ __forceinline__ float ipow(float b, int e) {
+  float r = 1.0f;
+  while (e > 0) {
+    if (e & 1) r *= b;
+    b *= b;
+    e >>= 1;
+  }
+  return r;
+}
+
+// Spiky gradient factor: grad_i W(r_vec) = f * r_vec, f = -S (h-r)^2 / r.
+__device__ __forceinline__ float spiky_factor(float r2, const PaperConsts &c) {
+  const float rinv = rsqrtf(r2);
+  const float hr = c.h - r2 * rinv;
+  return -c.spiky * hr * hr * rinv;
+}
+
+struct LambdaAcc {
+  float rho, gx, gy, gz, s;
+  __device__ __forceinline__ void add(float rx, float ry, float rz, float r2,
+                                      const PaperConsts &c) {
+    const float t = c.h2 - r2;
+    rho += c.poly6 * t * t * t;
+    const float f = spiky_factor(r2, c);
+    gx += f * rx;
+    gy += f * ry;
+    gz += f * rz;
+    s += f * f * r2;
+  }
+  __device__ __forceinline__ float lambda(const PaperConsts &c) const {
+    const float C = rho * c.inv_rho0 - 1.0f;
+    const float den = (gx * gx + gy * gy + gz * gz + s) * (c.inv_rho0 * c.inv_rho0);
+    return -C / (den + c.relax_eps);
+  }
+};
+
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+    k_predict_hash(const float4 *__restrict__ X, const float4 *__restrict__ V,
+                   uint32_t n, PaperConsts c,
+                   const SceneDesc *__restrict__ scenes,
+                   const uint16_t *__restrict__ sid, uint32_t *__restrict__ keys,
+                   uint32_t passes, uint32_t *__restrict__ hist) {
+  __shared__ uint32_t s_hist[kMaxSortPasses * kRadix];
+  for (uint32_t i = threadIdx.x; i < passes * kRadix; i += blockDim.x) s_hist[i] = 0;
+  __syncthreads();
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = k < n;
+  uint32_t key = 0;
+  if (valid) {
+    const float4 x = X[k];
+    const float4 v1 = gravity_velocity(V[k], c.dt, c.gy);
+    const float3 p = add3(x, displacement(v1, c.dt));
+    const SceneDesc &s = scene_of(scenes, sid, k);
+    key = s.cell_base + scene_cell(p.x, p.y, p.z, s);
+    keys[k] = key;
+  }
+  warp_digit_histogram(key, valid, passes, s_hist);
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < passes * kRadix; i += blockDim.x)
+    if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
+}
+
+__global__ void __launch_bounds__(256)
+    k_reorder(const uint32_t *__restrict__ perm, const float4 *__restrict__ X,
+              const float4 *__restrict__ V, const uint32_t *__restrict__ ID,
+              uint32_t n, PaperConsts c, float4 *__restrict__ X2,
+              float4 *__restrict__ V2, uint32_t *__restrict__ ID2,
+              float4 *__restrict__ P, float4 *__restrict__ D) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  // perm is a permutation of [0, n) unless the sort reported an error.
+  const uint32_t src = min(perm[k], n - 1);
+  const float4 x = X[src];
+  const float4 v1 = gravity_velocity(V[src], c.dt, c.gy);
+  const float3 d = displacement(v1, c.dt);
+  const float3 p = add3(x, d);
+  X2[k] = x;
+  V2[k] = v1;
+  ID2[k] = ID[src];
+  P[k] = make_float4(p.x, p.y, p.z, 0.0f);
+  D[k] = make_float4(d.x, d.y, d.z, 0.0f);
+}
+
+__global__ void __launch_bounds__(kGatherThreads)
+    k_nbr_lambda(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
+                 uint32_t *__restrict__ nbr, uint32_t *__restrict__ nbr_cnt,
+                 float4 *__restrict__ Q, float *__restrict__ R) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= c.n) return;
+  const float4 pk = P[k];
+  const SceneDesc &sc = scene_of(nc.scenes, nc.sid, k);
+  LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
+  uint32_t cnt = 0;
+  scan_cells(k, nc.skeys[k], sc, nc.off, [&](uint32_t j) {
+    const float4 pj = __ldg(&P[j]);
+    const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
+    const float r2 = rx * rx + ry * ry + rz * rz;
+    if (r2 > 0.0f && r2 < c.h2) {
+      if (cnt < c.maxn) nbr[(size_t)cnt * c.n + k] = j;
+      ++cnt;
+      acc.add(rx, ry, rz, r2, c);
+    }
+  });
+  nbr_cnt[k] = cnt;
+  Q[k] = make_float4(pk.x, pk.y, pk.z, acc.lambda(c));
+  R[k] = acc.rho;
+}
+
+__global__ void __launch_bounds__(kGatherThreads)
+    k_lambda(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
+             float4 *__restrict__ Q, float *__restrict__ R) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= c.n) return;
+  const float4 pk = P[k];
+  LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
+  visit_neighbours(nc, k, nc.cnt[k], [&](uint32_t j) {
+    const float4 pj = __ldg(&P[j]);
+    const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
+    const float r2 = rx * rx + ry * ry + rz * rz;
+    if (r2 > 0.0f && r2 < c.h2) acc.add(rx, ry, rz, r2, c);
+  });
+  Q[k] = make_float4(pk.x, pk.y, pk.z, acc.lambda(c));
+  R[k] = acc.rho;
+}
+
+__global__ void __launch_bounds__(kGatherThreads)
+    k_delta(const float4 *__restrict__ Q, NbrCtx nc, PaperConsts c,
+            float4 *__restrict__ D, float4 *__restrict__ P,
+            const float *__restrict__ R, float4 *__restrict__ U, int last) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= c.n) return;
+  const float4 qk = Q[k];
+  float sx = 0.f, sy = 0.f, sz = 0.f;
+  visit_neighbours(nc, k, nc.cnt[k], [&](uint32_t j) {
+    const float4 qj = __ldg(&Q[j]);
+    const float rx = qk.x - qj.x, ry = qk.y - qj.y, rz = qk.z - qj.z;
+    const float r2 = rx * rx + ry * ry + rz * rz;
+    if (r2 > 0.0f && r2 < c.h2) {
+      const float f = spiky_factor(r2, c);
+      const float ratio = (c.h2 - r2) * c.inv_scorr_den;
+      const float scorr = -c.scorr_k * ipow(ratio, c.scorr_n3);
+      const float w = (qk.w + qj.w + scorr) * f;
+      sx += w * rx;
+      sy += w * ry;
+      sz += w * rz;
+    }
+  });
+  const float4 x = nc.X2[k];
+  const float4 d0 = D[k];
+  float3 d = make_float3(d0.x + sx * c.inv_rho0, d0.y + sy * c.inv_rho0,
+                         d0.z + sz * c.inv_rho0);
+  float3 p = add3(x, d);
+  const SceneDesc &sc = scene_of(nc.scenes, nc.sid, k);
+  const float lo_x = sc.lo[0] + sc.wave;
+  // Collision response: clamp to the admissible box (moving x-min wall).
+  if (p.x < lo_x) { d.x = lo_x - x.x; p.x = x.x + d.x; }
+  else if (p.x > sc.hi[0]) { d.x = sc.hi[0] - x.x; p.x = x.x + d.x; }
+  if (p.y < sc.lo[1]) { d.y = sc.lo[1] - x.y; p.y = x.y + d.y; }
+  else if (p.y > sc.hi[1]) { d.y = sc.hi[1] - x.y; p.y = x.y + d.y; }
+  if (p.z < sc.lo[2]) { d.z = sc.lo[2] - x.z; p.z = x.z + d.z; }
+  else if (p.z > sc.hi[2]) { d.z = sc.hi[2] - x.z; p.z = x.z + d.z; }
+  D[k] = make_float4(d.x, d.y, d.z, 0.0f);
+  P[k] = make_float4(p.x, p.y, p.z, 0.0f);
+  if (last)
+    U[k] = make_float4(__fdiv_rn(d.x, c.dt), __fdiv_rn(d.y, c.dt),
+                       __fdiv_rn(d.z, c.dt), 1.0f / R[k]);
+}
+
+__global__ void __launch_bounds__(kGatherThreads)
+    k_vorticity(const float4 *__restrict__ P, const float4 *__restrict__ U,
+                NbrCtx nc, PaperConsts c, float4 *__restrict__ Wo) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= c.n) return;
+  const float4 pk = P[k];
+  const float4 uk = U[k];
+  float wx = 0.f, wy = 0.f, wz = 0.f;
+  visit_neighbours(nc, k, nc.cnt[k], [&](uint32_t j) {
+    const float4 pj = __ldg(&P[j]);
+    const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
+    const float r2 = rx * rx + ry * ry + rz * rz;
+    if (r2 > 0.0f && r2 < c.h2) {
+      const float4 uj = __ldg(&U[j]);
+      const float f = spiky_factor(r2, c) * uj.w;
+      const float gx = f * rx, gy = f * ry, gz = f * rz;
+      const float ux = uj.x - uk.x, uy = uj.y - uk.y, uz = uj.z - uk.z;
+      wx += gy * uz - gz * uy;
+      wy += gz * ux - gx * uz;
+      wz += gx * uy - gy * ux;
+    }
+  });
+  Wo[k] = make_float4(wx, wy, wz, sqrtf(wx * wx + wy * wy + wz * wz));
+}
+
+__global__ void __launch_bounds__(kGatherThreads)
+    k_xsph_commit(const float4 *__restrict__ P, const float4 *__restrict__ U,
+                  const float4 *__restrict__ Wv, NbrCtx nc, PaperConsts c,
+                  const uint32_t *__restrict__ ID2, float4 *__restrict__ X,
+                  float4 *__restrict__ V, uint32_t *__restrict__ ID) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= c.n) return;
+  const float4 pk = P[k];
+  const float4 uk = U[k];
+  const float4 wk = Wv[k];
+  float ex = 0.f, ey = 0.f, ez = 0.f, xx = 0.f, xy = 0.f, xz = 0.f;
+  visit_neighbours(nc, k, nc.cnt[k], [&](uint32_t j) {
+    const float4 pj = __ldg(&P[j]);
+    const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
+    const float r2 = rx * rx + ry * ry + rz * rz;
+    if (r2 > 0.0f && r2 < c.h2) {
+      const float4 uj = __ldg(&U[j]);
+      const float wn = __ldg(&Wv[j].w);
+      const float e = spiky_factor(r2, c) * uj.w * (wn - wk.w);
+      ex += e * rx;
+      ey += e * ry;
+      ez += e * rz;
+      const float t = c.h2 - r2;
+      const float wp = c.poly6 * t * t * t * uj.w;
+      xx += wp * (uj.x - uk.x);
+      xy += wp * (uj.y - uk.y);
+      xz += wp * (uj.z - uk.z);
+    }
+  });
+  const float el2 = ex * ex + ey * ey + ez * ez;
+  float nx = 0.f, ny = 0.f, nz = 0.f;
+  if (el2 > 0.0f) {
+    const float inv = rsqrtf(el2);
+    nx = ex * inv;
+    ny = ey * inv;
+    nz = ez * inv;
+  }
+  const float fx = c.vort_eps * (ny * wk.z - nz * wk.y);
+  const float fy = c.vort_eps * (nz * wk.x - nx * wk.z);
+  const float fz = c.vort_eps * (nx * wk.y - ny * wk.x);
+  const float vx = uk.x + c.dt * fx + c.xsph_c * xx;
+  const float vy = uk.y + c.dt * fy + c.xsph_c * xy;
+  const float vz = uk.z + c.dt * fz + c.xsph_c * xz;
+  X[k] = make_float4(pk.x, pk.y, pk.z, sqrtf(vx * vx + vy * vy + vz * vz));
+  V[k] = make_float4(vx, vy, vz, nc.V2[k].w);
+  ID[k] = ID2[k];
+}
+
+__global__ void k_gather_out(const float4 *__restrict__ X,
+                             const float4 *__restrict__ V,
+                             const uint32_t *__restrict__ ID, uint32_t n,
+                             float4 *__restrict__ out_pos,
+                             float4 *__restrict__ out_vel) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t i = ID[k];
+  out_pos[i] = X[k];
+  out_vel[i] = V[k];
+}
+
+__global__ void k_scatter_in(const float4 *__restrict__ in_pos,
+                             const float4 *__restrict__ in_vel,
+                             const uint32_t *__restrict__ ID, uint32_t n,
+                             float4 *__restrict__ X, float4 *__restrict__ V) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t i = ID[k];
+  X[k] = in_pos[i];
+  V[k] = in_vel[i];
+}
+
+__global__ void k_gather_scalar(const float *__restrict__ src,
+                                const uint32_t *__restrict__ ID, uint32_t n,
+                                float *__restrict__ out) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  out[ID[k]] = src[k];
+}
+
+__global__ void k_iota(uint32_t *__restrict__ dst, uint32_t n) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[k] = k;
+}
+
+inline uint32_t blocks_for(uint64_t n, uint32_t t) {
+  return (uint32_t)((n + t - 1) / t);
+}
+
+NbrCtx make_ctx(const DeviceState &d, const PaperConsts &c,
+                const uint16_t *sid) {
+  NbrCtx nc;
+  nc.nbr = d.nbr;
+  nc.cnt = d.nbr_cnt;
+  nc.skeys = d.skeys;
+  nc.off = d.offsets;
+  nc.X2 = d.X2;
+  nc.V2 = d.V2;
+  nc.scenes = d.scenes;
+  nc.sid = sid;
+  nc.n = c.n;
+  nc.maxn = c.maxn;
+  nc.dt = c.dt;
+  nc.h2 = c.h2;
+  return nc;
+}
+
+}  // namespace
+
+cudaError_t paper_predict_hash(const float4 *X, const float4 *V, uint32_t n,
+                               const PaperConsts &c, const SceneDesc *scenes,
+                               const uint16_t *sid, uint32_t *keys,
+                               const SortPlan &plan, uint32_t *sort_scratch,
+                               cudaStream_t st) {
+  k_predict_hash<<<blocks_for(n, 256), 256, 0, st>>>(
+      X, V, n, c, scenes, sid, keys, plan.passes, sort_scratch + plan.off_hist);
+  return cudaGetLastError();
+}
+
+cudaError_t paper_reorder(const uint32_t *perm, const float4 *X,
+                          const float4 *V, const uint32_t *ID, uint32_t n,
+                          const PaperConsts &c, float4 *X2, float4 *V2,
+                          uint32_t *ID2, float4 *P, float4 *D,
+                          cudaStream_t st) {
+  k_reorder<<<blocks_for(n, 256), 256, 0, st>>>(perm, X, V, ID, n, c, X2, V2,
+                                                 ID2, P, D);
+  return cudaGetLastError();
+}
+
+cudaError_t paper_nbr_lambda(const DeviceState &d, const PaperConsts &c,
+                             const uint16_t *sid, cudaStream_t st) {
+  k_nbr_lambda<<<blocks_for(c.n, kGatherThreads), kGatherThreads, 0, st>>>(
+      d.P, make_ctx(d, c, sid), c, d.nbr, d.nbr_cnt, d.Q, d.R);
+  return cudaGetLastError();
+}
+
+cudaError_t paper_lambda(const DeviceState &d, const PaperConsts &c,
+                         const uint16_t *sid, cudaStream_t st) {
+  k_lambda<<<blocks_for(c.n, kGatherThreads), kGatherThreads, 0, st>>>(
+      d.P, make_ctx(d, c, sid), c, d.Q, d.R);
+  return cudaGetLastError();
+}
+
+cudaError_t paper_delta(const DeviceState &d, const PaperConsts &c,
+                        const uint16_t *sid, bool last, cudaStream_t st) {
+  k_delta<<<blocks_for(c.n, kGatherThreads), kGatherThreads, 0, st>>>(
+      d.Q, make_ctx(d, c, sid), c, d.D, d.P, d.R, d.U, last ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t paper_vorticity(const DeviceState &d, const PaperConsts &c,
+                            const uint16_t *sid, cudaStream_t st) {
+  k_vorticity<<<blocks_for(c.n, kGatherThreads), kGatherThreads, 0, st>>>(
+      d.P, d.U, make_ctx(d, c, sid), c, d.W);
+  return cudaGetLastError();
+}
+
+cudaError_t paper_xsph_commit(const DeviceState &d, const PaperConsts &c,
+                              const uint16_t *sid, cudaStream_t st) {
+  k_xsph_commit<<<blocks_for(c.n, kGatherThreads), kGatherThreads, 0, st>>>(
+      d.P, d.U, d.W, make_ctx(d, c, sid), c, d.ID2, d.X, d.V, d.ID);
+  return cudaGetLastError();
+}
+
+cudaError_t gather_to_input_order(const float4 *X, const float4 *V,
+                                  const uint32_t *ID, uint32_t n,
+                                  float4 *out_pos, float4 *out_vel,
+                                  cudaStream_t st) {
+  k_gather_out<<<blocks_for(n, 256), 256, 0, st>>>(X, V, ID, n, out_pos, out_vel);
+  return cudaGetLastError();
+}
+
+cudaError_t scatter_from_input_order(const float4 *in_pos,
+                                     const float4 *in_vel, const uint32_t *ID,
+                                     uint32_t n, float4 *X, float4 *V,
+                                     cudaStream_t st) {
+  k_scatter_in<<<blocks_for(n, 256), 256, 0, st>>>(in_pos, in_vel, ID, n, X, V);
+  return cudaGetLastError();
+}
+
+cudaError_t gather_scalar_to_input_order(const float *src, const uint32_t *ID,
+                                         uint32_t n, float *out,
+                                         cudaStream_t st) {
+  k_gather_scalar<<<blocks_for(n, 256), 256, 0, st>>>(src, ID, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t iota_u32(uint32_t *dst, uint32_t n, cudaStream_t st) {
+  k_iota<<<blocks_for(n, 256), 256, 0, st>>>(dst, n);
+  return cudaGetLastError();
+}
+
+}  // namespace pbf

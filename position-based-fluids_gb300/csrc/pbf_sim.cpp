@@ -1,0 +1,631 @@
+// The single-scene simulation object behind the C-ABI (include/pbf.h) and
+// the neighbour-structure operator entry points.
+//
+// Reference: Simulation (src/Simulation.hpp:41-108, src/Simulation.cpp):
+// construction (:34-88), init (:104-201), initCells (:203-230), step
+// (:455-576), dumpData (:578-591), setWaveGenerator (Simulation.hpp:105-108).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "pbf_host.hpp"
+
+using namespace pbf;
+
+namespace {
+struct KernelTime {
+  double ms = 0;
+  uint64_t launches = 0;
+  uint64_t groups = 0;
+};
+}  // namespace
+
+struct pbf_sim {
+  pbf_params prm{};
+  uint32_t n = 0;
+  std::vector<pbf_particle> particles;
+  bool paper = true;
+  bool inited = false;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DeviceState d;
+  PaperConsts pc{};
+  RefConsts rc{};
+  SceneDesc scene{};
+  SortPlan plan;
+  uint32_t ncells = 0;
+  std::vector<void *> allocations;
+  size_t device_bytes = 0;
+  // CUDA graph of one step
+  bool use_graph = true;
+  cudaGraphExec_t graph = nullptr;
+  // per-stage timing
+  bool timing = false;
+  std::vector<cudaEvent_t> events;
+  std::vector<int> event_stage;
+  std::vector<const char *> event_name;
+  std::vector<uint32_t> event_launches;
+  size_t events_used = 0;
+  double stage_acc[4] = {0, 0, 0, 0};
+  uint32_t timed_steps = 0;
+  std::map<std::string, KernelTime> kernel_times;
+  float stage_ms[4] = {0, 0, 0, 0};
+  bool have_times = false;
+  bool stepped = false;
+  bool scene_dirty = false;
+  // debug views
+  int32_t *d_ranges = nullptr;
+};
+
+namespace {
+
+template <typename T>
+int dalloc(pbf_sim *s, T **p, size_t count) {
+  void *q = nullptr;
+  const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) return cuda_status(e, "cudaMalloc");
+  s->allocations.push_back(q);
+  s->device_bytes += bytes;
+  *p = static_cast<T *>(q);
+  return PBF_OK;
+}
+
+void free_all(pbf_sim *s) {
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  s->graph = nullptr;
+  for (cudaEvent_t e : s->events) cudaEventDestroy(e);
+  s->events.clear();
+  for (void *p : s->allocations) cudaFree(p);
+  s->allocations.clear();
+  if (s->stream) cudaStreamDestroy(s->stream);
+  s->stream = nullptr;
+}
+
+#define PBF_TRY(expr)                                  \
+  do {                                                 \
+    const cudaError_t e_ = (expr);                     \
+    if (e_ != cudaSuccess) return cuda_status(e_, #expr); \
+  } while (0)
+
+#define PBF_TRY_STATUS(expr)      \
+  do {                            \
+    const int s_ = (expr);        \
+    if (s_ != PBF_OK) return s_;  \
+  } while (0)
+
+// Records a boundary after a launch when timing is on: `stage` is one of the
+// four reported stages (-1 = start of step), `name` the kernel (or kernel
+// group) that just ran and `launches` how many launches that group was.
+int mark(pbf_sim *s, int stage, const char *name, uint32_t launches,
+         size_t *next) {
+  if (!s->timing) return PBF_OK;
+  if (*next >= s->events.size()) {
+    cudaEvent_t e;
+    PBF_TRY(cudaEventCreate(&e));
+    s->events.push_back(e);
+    s->event_stage.push_back(stage);
+    s->event_name.push_back(name);
+    s->event_launches.push_back(launches);
+  }
+  s->event_stage[*next] = stage;
+  s->event_name[*next] = name;
+  s->event_launches[*next] = launches;
+  PBF_TRY(cudaEventRecord(s->events[*next], s->stream));
+  ++*next;
+  return PBF_OK;
+}
+
+int launch_step(pbf_sim *s) {
+  DeviceState &d = s->d;
+  const cudaStream_t st = s->stream;
+  const uint32_t n = s->n;
+  const uint32_t passes = s->plan.passes;
+  size_t ev = 0;
+  s->events_used = 0;
+  PBF_TRY_STATUS(mark(s, -1, "start", 0, &ev));
+  PBF_TRY(sort_clear(s->plan, d.sort_scratch, st));
+  if (s->paper) {
+    PBF_TRY(paper_predict_hash(d.X, d.V, n, s->pc, d.scenes, nullptr, d.keys,
+                               s->plan, d.sort_scratch, st));
+    PBF_TRY_STATUS(mark(s, 0, "predict_hash", 1, &ev));
+    PBF_TRY(sort_scan(s->plan, d.sort_scratch, st));
+    PBF_TRY(sort_passes(s->plan, d.keys, nullptr, d.skeys, d.perm,
+                        d.sort_scratch, d.err, st));
+    PBF_TRY_STATUS(mark(s, 0, "sort_onesweep", 1 + passes, &ev));
+    PBF_TRY(cell_offsets(d.skeys, n, s->ncells, d.offsets, st));
+    PBF_TRY_STATUS(mark(s, 0, "cell_offsets", 1, &ev));
+    PBF_TRY(paper_reorder(d.perm, d.X, d.V, d.ID, n, s->pc, d.X2, d.V2, d.ID2,
+                          d.P, d.D, st));
+    PBF_TRY_STATUS(mark(s, 0, "reorder", 1, &ev));
+    const uint32_t iters = s->prm.solver_iterations;
+    for (uint32_t it = 0; it < iters; ++it) {
+      if (it == 0) {
+        PBF_TRY(paper_nbr_lambda(d, s->pc, nullptr, st));
+        PBF_TRY_STATUS(mark(s, 1, "nbr_lambda", 1, &ev));
+      } else {
+        PBF_TRY(paper_lambda(d, s->pc, nullptr, st));
+        PBF_TRY_STATUS(mark(s, 1, "lambda", 1, &ev));
+      }
+      PBF_TRY(paper_delta(d, s->pc, nullptr, it + 1 == iters, st));
+      PBF_TRY_STATUS(mark(s, 2, "delta", 1, &ev));
+    }
+    PBF_TRY(paper_vorticity(d, s->pc, nullptr, st));
+    PBF_TRY_STATUS(mark(s, 3, "vorticity", 1, &ev));
+    PBF_TRY(paper_xsph_commit(d, s->pc, nullptr, st));
+    PBF_TRY_STATUS(mark(s, 3, "xsph_commit", 1, &ev));
+  } else {
+    PBF_TRY(rc_predict_hash(d.X, d.V, d.P, n, s->rc, d.scenes, d.keys, s->plan,
+                            d.sort_scratch, st));
+    PBF_TRY_STATUS(mark(s, 0, "rc_predict_hash", 1, &ev));
+    PBF_TRY(sort_scan(s->plan, d.sort_scratch, st));
+    PBF_TRY(sort_passes(s->plan, d.keys, nullptr, d.skeys, d.perm,
+                        d.sort_scratch, d.err, st));
+    PBF_TRY_STATUS(mark(s, 0, "sort_onesweep", 1 + passes, &ev));
+    PBF_TRY(cell_offsets(d.skeys, n, s->ncells, d.offsets, st));
+    PBF_TRY_STATUS(mark(s, 0, "cell_offsets", 1, &ev));
+    float4 *cur = d.P, *alt = d.P2;
+    const uint32_t iters = s->prm.solver_iterations;
+    for (uint32_t it = 0; it < iters; ++it) {
+      PBF_TRY(rc_lambda(cur, d.S, d.perm, d.offsets, n, s->rc, st));
+      PBF_TRY_STATUS(mark(s, 1, "rc_lambda", 1, &ev));
+      PBF_TRY(rc_delta(cur, alt, d.S, d.perm, d.offsets, d.X, d.V, n, s->rc,
+                       d.scenes, it + 1 == iters, st));
+      PBF_TRY_STATUS(mark(s, 2, "rc_delta", 1, &ev));
+      std::swap(cur, alt);
+    }
+    if (cur != d.P)
+      PBF_TRY(cudaMemcpyAsync(d.P, cur, (size_t)n * sizeof(float4),
+                              cudaMemcpyDeviceToDevice, st));
+    PBF_TRY(rc_xsph(d.P, d.V, d.DV, d.perm, d.offsets, n, s->rc, st));
+    PBF_TRY_STATUS(mark(s, 3, "rc_xsph", 1, &ev));
+    PBF_TRY(rc_commit(d.X, d.V, d.P, d.DV, n, st));
+    PBF_TRY_STATUS(mark(s, 3, "rc_commit", 1, &ev));
+  }
+  s->events_used = ev;
+  return PBF_OK;
+}
+
+int upload_scene(pbf_sim *s) {
+  PBF_TRY(cudaMemcpyAsync(s->d.scenes, &s->scene, sizeof(SceneDesc),
+                          cudaMemcpyHostToDevice, s->stream));
+  s->scene_dirty = false;
+  return PBF_OK;
+}
+
+int check_device_error(pbf_sim *s) {
+  uint32_t flag = 0;
+  PBF_TRY(cudaMemcpyAsync(&flag, s->d.err, sizeof flag, cudaMemcpyDeviceToHost,
+                          s->stream));
+  PBF_TRY(cudaStreamSynchronize(s->stream));
+  if (flag) {
+    PBF_TRY(cudaMemsetAsync(s->d.err, 0, sizeof(uint32_t), s->stream));
+    PBF_TRY(cudaStreamSynchronize(s->stream));
+    set_error_message("device error flag " + std::to_string(flag));
+    return PBF_ERR_DEVICE;
+  }
+  return PBF_OK;
+}
+
+int build_graph(pbf_sim *s) {
+  if (s->graph) return PBF_OK;
+  cudaGraph_t g = nullptr;
+  PBF_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  const bool was_timing = s->timing;
+  s->timing = false;
+  const int rc = launch_step(s);
+  s->timing = was_timing;
+  const cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+  if (rc != PBF_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture");
+  const cudaError_t ie = cudaGraphInstantiate(&s->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) {
+    s->graph = nullptr;
+    return cuda_status(ie, "cudaGraphInstantiate");
+  }
+  return PBF_OK;
+}
+
+// Accumulates the stage and per-kernel times of the step just launched.
+int collect_times(pbf_sim *s) {
+  if (s->events_used < 2) return PBF_OK;
+  PBF_TRY(cudaEventSynchronize(s->events[s->events_used - 1]));
+  for (size_t q = 1; q < s->events_used; ++q) {
+    float ms = 0;
+    PBF_TRY(cudaEventElapsedTime(&ms, s->events[q - 1], s->events[q]));
+    const int st = s->event_stage[q];
+    if (st >= 0 && st < 4) s->stage_acc[st] += ms;
+    KernelTime &kt = s->kernel_times[s->event_name[q]];
+    kt.ms += ms;
+    kt.launches += s->event_launches[q];
+    kt.groups += 1;
+  }
+  s->timed_steps += 1;
+  for (int st = 0; st < 4; ++st) s->stage_ms[st] = (float)(s->stage_acc[st] / s->timed_steps);
+  s->have_times = true;
+  return PBF_OK;
+}
+
+bool ready(const pbf_sim *s) { return s && s->inited; }
+
+}  // namespace
+
+extern "C" {
+
+int pbf_create(const pbf_params *params, const pbf_particle *particles,
+               uint32_t n, pbf_sim **out) {
+  if (!params || !out || (!particles && n)) return PBF_ERR_INVALID;
+  *out = nullptr;
+  const int v = validate_params(*params, n);
+  if (v != PBF_OK) return v;
+  std::unique_ptr<pbf_sim> s(new pbf_sim());
+  s->prm = *params;
+  s->n = n;
+  s->particles.assign(particles, particles + n);
+  s->paper = params->mode == PBF_MODE_PAPER;
+  s->ncells = (uint32_t)grid_cells(*params);
+  s->scene = make_scene(*params);
+  s->rc = make_ref_consts(*params);
+  s->rc.n = n;
+  s->pc = make_paper_consts(*params, n);
+  s->plan = make_sort_plan(n, bits_for(s->ncells));
+  *out = s.release();
+  return PBF_OK;
+}
+
+int pbf_init(pbf_sim *s) {
+  if (!s) return PBF_ERR_INVALID;
+  if (s->inited) return PBF_ERR_STATE;
+  PBF_TRY(cudaGetDevice(&s->device));
+  PBF_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  DeviceState &d = s->d;
+  const size_t n = s->n;
+  int rc = PBF_OK;
+  auto A = [&](auto **p, size_t count) {
+    if (rc == PBF_OK) rc = dalloc(s, p, count);
+  };
+  A(&d.X, n);
+  A(&d.V, n);
+  A(&d.P, n);
+  A(&d.keys, n);
+  A(&d.skeys, n);
+  A(&d.perm, n);
+  A(&d.offsets, (size_t)s->ncells + 1);
+  A(&d.sort_scratch, s->plan.words);
+  A(&d.err, 1);
+  A(&d.scenes, 1);
+  A(&d.io_pos, n);
+  A(&d.io_vel, n);
+  if (s->paper) {
+    A(&d.ID, n);
+    A(&d.ID2, n);
+    A(&d.X2, n);
+    A(&d.V2, n);
+    A(&d.Q, n);
+    A(&d.D, n);
+    A(&d.U, n);
+    A(&d.W, n);
+    A(&d.R, n);
+    A(&d.nbr_cnt, n);
+    A(&d.nbr, (size_t)s->prm.max_neighbours * n);
+  } else {
+    A(&d.P2, n);
+    A(&d.DV, n);
+    A(&d.S, n);
+  }
+  if (rc != PBF_OK) {
+    free_all(s);
+    return rc;
+  }
+  // Initial state in the dumpData layout (src/Simulation.cpp:120-134).
+  std::vector<float4> pos(n), vel(n);
+  for (size_t i = 0; i < n; ++i) {
+    const pbf_particle &p = s->particles[i];
+    pos[i] = make_float4(p.x[0], p.x[1], p.x[2], 0.0f);
+    vel[i] = make_float4(p.v[0], p.v[1], p.v[2], p.m);
+  }
+  PBF_TRY(cudaMemsetAsync(d.err, 0, sizeof(uint32_t), s->stream));
+  PBF_TRY(cudaMemsetAsync(d.P, 0, n * sizeof(float4), s->stream));
+  PBF_TRY(cudaMemsetAsync(d.offsets, 0, ((size_t)s->ncells + 1) * sizeof(uint32_t),
+                          s->stream));
+  PBF_TRY(cudaMemcpyAsync(d.X, pos.data(), n * sizeof(float4),
+                          cudaMemcpyHostToDevice, s->stream));
+  PBF_TRY(cudaMemcpyAsync(d.V, vel.data(), n * sizeof(float4),
+                          cudaMemcpyHostToDevice, s->stream));
+  if (s->paper) PBF_TRY(iota_u32(d.ID, s->n, s->stream));
+  PBF_TRY_STATUS(upload_scene(s));
+  PBF_TRY(cudaStreamSynchronize(s->stream));
+  s->inited = true;
+  return PBF_OK;
+}
+
+int pbf_init_cells(pbf_sim *s) { return ready(s) ? PBF_OK : PBF_ERR_STATE; }
+
+int pbf_step(pbf_sim *s, uint32_t nsteps) {
+  if (!ready(s)) return PBF_ERR_STATE;
+  for (uint32_t k = 0; k < nsteps; ++k) {
+    if (s->scene_dirty) PBF_TRY_STATUS(upload_scene(s));
+    if (s->timing) {
+      PBF_TRY_STATUS(launch_step(s));
+      PBF_TRY_STATUS(collect_times(s));
+    } else if (s->use_graph) {
+      PBF_TRY_STATUS(build_graph(s));
+      PBF_TRY(cudaGraphLaunch(s->graph, s->stream));
+    } else {
+      PBF_TRY_STATUS(launch_step(s));
+    }
+    s->stepped = true;
+  }
+  return PBF_OK;
+}
+
+int pbf_sync(pbf_sim *s) {
+  if (!ready(s)) return PBF_ERR_STATE;
+  return check_device_error(s);
+}
+
+int pbf_set_state_async(pbf_sim *s, const float *pos4, const float *vel4) {
+  if (!ready(s) || !pos4 || !vel4) return ready(s) ? PBF_ERR_INVALID : PBF_ERR_STATE;
+  DeviceState &d = s->d;
+  const size_t bytes = (size_t)s->n * sizeof(float4);
+  if (s->paper) {
+    PBF_TRY(cudaMemcpyAsync(d.io_pos, pos4, bytes, cudaMemcpyHostToDevice, s->stream));
+    PBF_TRY(cudaMemcpyAsync(d.io_vel, vel4, bytes, cudaMemcpyHostToDevice, s->stream));
+    PBF_TRY(scatter_from_input_order(d.io_pos, d.io_vel, d.ID, s->n, d.X, d.V,
+                                     s->stream));
+  } else {
+    PBF_TRY(cudaMemcpyAsync(d.X, pos4, bytes, cudaMemcpyHostToDevice, s->stream));
+    PBF_TRY(cudaMemcpyAsync(d.V, vel4, bytes, cudaMemcpyHostToDevice, s->stream));
+  }
+  return PBF_OK;
+}
+
+int pbf_dump_data_async(pbf_sim *s, float *pos4, float *vel4) {
+  if (!ready(s) || !pos4 || !vel4) return ready(s) ? PBF_ERR_INVALID : PBF_ERR_STATE;
+  DeviceState &d = s->d;
+  const size_t bytes = (size_t)s->n * sizeof(float4);
+  const float4 *sp = d.X, *sv = d.V;
+  if (s->paper) {
+    PBF_TRY(gather_to_input_order(d.X, d.V, d.ID, s->n, d.io_pos, d.io_vel,
+                                  s->stream));
+    sp = d.io_pos;
+    sv = d.io_vel;
+  }
+  PBF_TRY(cudaMemcpyAsync(pos4, sp, bytes, cudaMemcpyDeviceToHost, s->stream));
+  PBF_TRY(cudaMemcpyAsync(vel4, sv, bytes, cudaMemcpyDeviceToHost, s->stream));
+  return PBF_OK;
+}
+
+int pbf_set_state(pbf_sim *s, const float *pos4, const float *vel4) {
+  PBF_TRY_STATUS(pbf_set_state_async(s, pos4, vel4));
+  PBF_TRY(cudaStreamSynchronize(s->stream));
+  return PBF_OK;
+}
+
+int pbf_dump_data(pbf_sim *s, float *pos4, float *vel4) {
+  PBF_TRY_STATUS(pbf_dump_data_async(s, pos4, vel4));
+  return check_device_error(s);
+}
+
+int pbf_host_alloc(size_t bytes, void **out) {
+  if (!out) return PBF_ERR_INVALID;
+  PBF_TRY(cudaMallocHost(out, bytes ? bytes : 16));
+  return PBF_OK;
+}
+
+int pbf_host_free(void *ptr) {
+  if (ptr) PBF_TRY(cudaFreeHost(ptr));
+  return PBF_OK;
+}
+
+int pbf_set_wave(pbf_sim *s, float value) {
+  if (!s) return PBF_ERR_INVALID;
+  s->scene.wave = value;
+  s->scene_dirty = true;
+  return PBF_OK;
+}
+
+int pbf_get_num_particles(const pbf_sim *s, uint32_t *n) {
+  if (!s || !n) return PBF_ERR_INVALID;
+  *n = s->n;
+  return PBF_OK;
+}
+
+int pbf_get_sizes(const pbf_sim *s, float min4[4], float max4[4]) {
+  if (!s || !min4 || !max4) return PBF_ERR_INVALID;
+  min4[0] = s->prm.x_min;
+  min4[1] = s->prm.y_min;
+  min4[2] = s->prm.z_min;
+  min4[3] = 0.0f;
+  max4[0] = s->prm.x_max;
+  max4[1] = s->prm.y_max;
+  max4[2] = s->prm.z_max;
+  max4[3] = 0.0f;
+  return PBF_OK;
+}
+
+int pbf_get_stream(const pbf_sim *s, void **stream) {
+  if (!s || !stream) return PBF_ERR_INVALID;
+  if (!s->inited) return PBF_ERR_STATE;
+  *stream = (void *)s->stream;
+  return PBF_OK;
+}
+
+int pbf_set_stage_timing(pbf_sim *s, int enable) {
+  if (!s) return PBF_ERR_INVALID;
+  s->timing = enable != 0;
+  s->kernel_times.clear();
+  for (double &a : s->stage_acc) a = 0;
+  s->timed_steps = 0;
+  s->have_times = false;
+  return PBF_OK;
+}
+
+int pbf_kernel_times(pbf_sim *s, uint32_t cap, char *names, float *total_ms,
+                     uint32_t *launches, uint32_t *count) {
+  if (!s || !count) return PBF_ERR_INVALID;
+  uint32_t q = 0;
+  for (const auto &kv : s->kernel_times) {
+    if (q < cap) {
+      if (names) {
+        std::strncpy(names + 32 * (size_t)q, kv.first.c_str(), 31);
+        names[32 * (size_t)q + 31] = '\0';
+      }
+      if (total_ms) total_ms[q] = (float)kv.second.ms;
+      if (launches) launches[q] = (uint32_t)kv.second.launches;
+    }
+    ++q;
+  }
+  *count = q;
+  return PBF_OK;
+}
+
+int pbf_stage_times(pbf_sim *s, float ms[4]) {
+  if (!s || !ms) return PBF_ERR_INVALID;
+  if (!s->have_times) return PBF_ERR_STATE;
+  std::memcpy(ms, s->stage_ms, sizeof s->stage_ms);
+  return PBF_OK;
+}
+
+int pbf_set_graph(pbf_sim *s, int enable) {
+  if (!s) return PBF_ERR_INVALID;
+  s->use_graph = enable != 0;
+  return PBF_OK;
+}
+
+int pbf_launches_per_step(const pbf_sim *s, uint32_t *launches) {
+  if (!s || !launches) return PBF_ERR_INVALID;
+  const uint32_t it = s->prm.solver_iterations;
+  const uint32_t sort = 1u /*scan*/ + s->plan.passes + 1u /*offsets*/;
+  if (s->paper)
+    *launches = 1u /*predict+hash*/ + sort + 1u /*reorder*/ + 2u * it + 2u;
+  else
+    *launches = 1u + sort + 2u * it + 2u;
+  return PBF_OK;
+}
+
+int pbf_get_density(pbf_sim *s, float *density) {
+  if (!ready(s) || !density) return ready(s) ? PBF_ERR_INVALID : PBF_ERR_STATE;
+  const size_t n = s->n;
+  if (s->paper) {
+    float *tmp = reinterpret_cast<float *>(s->d.io_pos);
+    PBF_TRY(gather_scalar_to_input_order(s->d.R, s->d.ID, s->n, tmp, s->stream));
+    PBF_TRY(cudaMemcpyAsync(density, tmp, n * sizeof(float),
+                            cudaMemcpyDeviceToHost, s->stream));
+    PBF_TRY(cudaStreamSynchronize(s->stream));
+  } else {
+    std::vector<float4> p(n);
+    PBF_TRY(cudaMemcpyAsync(p.data(), s->d.P, n * sizeof(float4),
+                            cudaMemcpyDeviceToHost, s->stream));
+    PBF_TRY(cudaStreamSynchronize(s->stream));
+    for (size_t i = 0; i < n; ++i) density[i] = p[i].w;
+  }
+  return PBF_OK;
+}
+
+int pbf_get_cells(pbf_sim *s, uint32_t *hash, uint32_t *perm, int32_t *ranges) {
+  if (!ready(s)) return PBF_ERR_STATE;
+  if (!s->stepped) return PBF_ERR_STATE;
+  const size_t n = s->n;
+  std::vector<uint32_t> skeys(n), p(n), id(n);
+  PBF_TRY(cudaMemcpyAsync(skeys.data(), s->d.skeys, n * 4, cudaMemcpyDeviceToHost, s->stream));
+  PBF_TRY(cudaMemcpyAsync(p.data(), s->paper ? s->d.ID : s->d.perm, n * 4,
+                          cudaMemcpyDeviceToHost, s->stream));
+  if (!s->paper && hash)
+    PBF_TRY(cudaMemcpyAsync(hash, s->d.keys, n * 4, cudaMemcpyDeviceToHost, s->stream));
+  if (ranges) {
+    if (!s->d_ranges) PBF_TRY_STATUS(dalloc(s, &s->d_ranges, 2 * (size_t)s->ncells));
+    PBF_TRY(find_cells(s->d.offsets, s->ncells, s->d_ranges, s->stream));
+    PBF_TRY(cudaMemcpyAsync(ranges, s->d_ranges, (size_t)s->ncells * 8,
+                            cudaMemcpyDeviceToHost, s->stream));
+  }
+  PBF_TRY(cudaStreamSynchronize(s->stream));
+  if (s->paper && hash)
+    for (size_t q = 0; q < n; ++q) hash[p[q]] = skeys[q];
+  if (perm) std::memcpy(perm, p.data(), n * 4);
+  return PBF_OK;
+}
+
+int pbf_destroy(pbf_sim *s) {
+  if (!s) return PBF_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  free_all(s);
+  delete s;
+  return PBF_OK;
+}
+
+/* ------------------------------------------------------------ operators */
+int pbf_op_cell_hash(const pbf_params *params, const float *d_pred4, uint32_t n,
+                     uint32_t *d_hash, void *stream) {
+  if (!params || (n && (!d_pred4 || !d_hash))) return PBF_ERR_INVALID;
+  if (grid_cells(*params) == 0 || grid_cells(*params) > (1ull << 31)) return PBF_ERR_INVALID;
+  const SceneDesc sc = make_scene(*params);
+  PBF_TRY(cell_hash(reinterpret_cast<const float4 *>(d_pred4), n, sc, d_hash,
+                    (cudaStream_t)stream));
+  return PBF_OK;
+}
+
+size_t pbf_op_sort_scratch_bytes(uint32_t n, uint32_t key_bits) {
+  return make_sort_plan(n, key_bits).words * sizeof(uint32_t);
+}
+
+int pbf_op_sort_pairs(const uint32_t *d_keys_in, const uint32_t *d_vals_in,
+                      uint32_t n, uint32_t key_bits, uint32_t *d_keys_out,
+                      uint32_t *d_vals_out, void *d_scratch,
+                      size_t scratch_bytes, void *stream) {
+  if (n == 0) return PBF_OK;
+  if (!d_keys_in || !d_keys_out || !d_vals_out || !d_scratch) return PBF_ERR_INVALID;
+  if (key_bits < 1 || key_bits > 32 || n >= (1u << 30)) return PBF_ERR_INVALID;
+  const SortPlan plan = make_sort_plan(n, key_bits);
+  if (scratch_bytes < plan.words * sizeof(uint32_t)) return PBF_ERR_INVALID;
+  uint32_t *scratch = static_cast<uint32_t *>(d_scratch);
+  uint32_t *err = scratch + plan.off_counter + 31;
+  const cudaStream_t st = (cudaStream_t)stream;
+  PBF_TRY(sort_clear(plan, scratch, st));
+  PBF_TRY(sort_histogram(plan, d_keys_in, scratch, st));
+  PBF_TRY(sort_scan(plan, scratch, st));
+  PBF_TRY(sort_passes(plan, d_keys_in, d_vals_in, d_keys_out, d_vals_out,
+                      scratch, err, st));
+  return PBF_OK;
+}
+
+int pbf_op_sort_status(const void *d_scratch, uint32_t n, uint32_t key_bits,
+                       void *stream) {
+  if (!d_scratch) return PBF_ERR_INVALID;
+  if (n == 0) return PBF_OK;
+  const SortPlan plan = make_sort_plan(n, key_bits);
+  uint32_t flag = 0;
+  const uint32_t *err = static_cast<const uint32_t *>(d_scratch) + plan.off_counter + 31;
+  PBF_TRY(cudaMemcpyAsync(&flag, err, 4, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  PBF_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  if (flag) {
+    set_error_message("radix sort look-back wait gave up");
+    return PBF_ERR_DEVICE;
+  }
+  return PBF_OK;
+}
+
+int pbf_op_cell_offsets(const uint32_t *d_sorted_keys, uint32_t n,
+                        uint32_t ncells, uint32_t *d_offsets, void *stream) {
+  if (!d_offsets || (n && !d_sorted_keys) || ncells == 0) return PBF_ERR_INVALID;
+  PBF_TRY(cell_offsets(d_sorted_keys, n, ncells, d_offsets, (cudaStream_t)stream));
+  return PBF_OK;
+}
+
+int pbf_op_find_cells(const uint32_t *d_offsets, uint32_t ncells,
+                      int32_t *d_first_last, void *stream) {
+  if (!d_offsets || !d_first_last) return PBF_ERR_INVALID;
+  PBF_TRY(find_cells(d_offsets, ncells, d_first_last, (cudaStream_t)stream));
+  return PBF_OK;
+}
+
+}  // extern "C"

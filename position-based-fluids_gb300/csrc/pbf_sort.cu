@@ -1,0 +1,362 @@
+// Neighbour structure for the GB300 position-based-fluids step: cell hash,
+// onesweep LSD radix sort of 32-bit cell keys, CSR cell offsets and the
+// reference's inclusive cell ranges.
+//
+// Reference semantics this implements (MrMagne/position-based-fluids):
+//   - cell hash: src/kernels/update_cells.cl:10-15 (and calc_hash.cl:15-20);
+//   - a stable LSD radix sort of (cell, particle index) pairs, the intent of
+//     src/kernels/radix_histogram.cl, radix_scan.cl, radix_paste.cl and
+//     radix_reorder.cl driven by src/Simulation.cpp:351-435 (that code does
+//     not run as shipped: radix_reorder.cl:28-41 uses an uninitialised
+//     counter);
+//   - inclusive [first,last] cell ranges with -1 for empty cells, the intent
+//     of init_cells.cl and find_cells.cl.
+//
+// The sort is the onesweep scheme (one upfront histogram pass for every
+// digit, then one pass per 8-bit digit that ranks a tile of keys with
+// warp-level multisplit, publishes per-digit tile counts and resolves its
+// global offsets by decoupled look-back).  Tiles are numbered by an atomic
+// counter in the order CTAs start, so a CTA only ever waits on tiles that
+// are already resident; every wait is additionally bounded, and a wait that
+// runs out sets a device error bit instead of spinning on.
+#include "pbf_device.cuh"
+
+namespace pbf {
+
+namespace {
+
+constexpr uint32_t kLbMask = (1u << 30) - 1u;
+constexpr uint32_t kLbAggregate = 1u << 30;
+constexpr uint32_t kLbInclusive = 2u << 30;
+constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr int kSortWarps = kSortThreads / 32;
+static_assert(kSortThreads == kRadix, "one thread per digit in the scan");
+
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) {
+  return *reinterpret_cast<const volatile uint32_t *>(p);
+}
+__device__ __forceinline__ void st_volatile(uint32_t *p, uint32_t v) {
+  *reinterpret_cast<volatile uint32_t *>(p) = v;
+}
+
+// Exclusive scan of one value per thread over a 256-thread block.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v,
+                                                         uint32_t *s_warp) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < kSortWarps ? s_warp[lane] : 0u;
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < kSortWarps; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += t;
+    }
+    if (lane < kSortWarps) s_warp[lane] = wi - w;
+  }
+  __syncthreads();
+  return incl - v + s_warp[warp];
+}
+
+__global__ void __launch_bounds__(256)
+    k_sort_histogram(const uint32_t *__restrict__ keys, uint32_t n,
+                     uint32_t passes, uint32_t *__restrict__ hist) {
+  __shared__ uint32_t s_hist[kMaxSortPasses * kRadix];
+  for (uint32_t i = threadIdx.x; i < passes * kRadix; i += blockDim.x) s_hist[i] = 0;
+  __syncthreads();
+  const uint32_t stride = gridDim.x * blockDim.x;
+  // Whole warps iterate together so that __match_any_sync sees every lane.
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    const bool valid = i < n;
+    warp_digit_histogram(valid ? keys[i] : 0u, valid, passes, s_hist);
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < passes * kRadix; i += blockDim.x)
+    if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
+}
+
+__global__ void __launch_bounds__(kSortThreads)
+    k_sort_scan(uint32_t passes, uint32_t *__restrict__ hist) {
+  __shared__ uint32_t s_warp[kSortWarps];
+  for (uint32_t p = 0; p < passes; ++p) {
+    const uint32_t v = hist[p * kRadix + threadIdx.x];
+    const uint32_t e = block_exclusive_scan(v, s_warp);
+    hist[p * kRadix + threadIdx.x] = e;
+    __syncthreads();
+  }
+}
+
+template <bool kIota>
+__global__ void __launch_bounds__(kSortThreads)
+    k_onesweep(const uint32_t *__restrict__ keys_in,
+               const uint32_t *__restrict__ vals_in,
+               uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out,
+               uint32_t n, uint32_t shift,
+               const uint32_t *__restrict__ global_excl,
+               uint32_t *lookback, uint32_t *tile_counter, uint32_t *err) {
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_wcnt[kSortWarps][kRadix];
+  __shared__ uint32_t s_dexcl[kRadix];
+  __shared__ uint32_t s_gbase[kRadix];
+  __shared__ uint32_t s_warp[kSortWarps];
+  __shared__ uint32_t s_keys[kSortTile];
+  __shared__ uint32_t s_vals[kSortTile];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_tile = atomicAdd(tile_counter, 1u);
+  for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads)
+    (&s_wcnt[0][0])[i] = 0u;
+  __syncthreads();
+
+  const uint32_t tile = s_tile;
+  const uint32_t tile_base = tile * (uint32_t)kSortTile;
+  // Each warp owns a contiguous segment of 32*kSortItems keys and reads it
+  // lane-striped; the warp-local order (item, lane) is the input order.
+  const uint32_t seg = tile_base + (uint32_t)warp * (32u * kSortItems);
+
+  uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+#pragma unroll
+  for (int it = 0; it < kSortItems; ++it) {
+    const uint32_t idx = seg + (uint32_t)it * 32u + lane;
+    const bool ok = idx < n;
+    key[it] = ok ? keys_in[idx] : 0u;
+    val[it] = ok ? (kIota ? idx : vals_in[idx]) : 0u;
+  }
+
+  // Warp-level multisplit: stable rank of each key among the warp's keys of
+  // the same digit, item by item.
+  const unsigned lt_mask = (1u << lane) - 1u;
+#pragma unroll
+  for (int it = 0; it < kSortItems; ++it) {
+    const uint32_t idx = seg + (uint32_t)it * 32u + lane;
+    const bool ok = idx < n;
+    const uint32_t d = (key[it] >> shift) & (kRadix - 1);
+    const unsigned peers = __match_any_sync(0xffffffffu, ok ? d : 0xffffffffu);
+    const uint32_t before = ok ? s_wcnt[warp][d] : 0u;
+    __syncwarp();
+    rank[it] = before + (uint32_t)__popc(peers & lt_mask);
+    if (ok && lane == 31 - __clz(peers))
+      s_wcnt[warp][d] = before + (uint32_t)__popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // Per digit: the tile's count, and each warp's exclusive offset.
+  const uint32_t d = (uint32_t)tid;
+  uint32_t tile_count = 0;
+#pragma unroll
+  for (int w = 0; w < kSortWarps; ++w) {
+    const uint32_t c = s_wcnt[w][d];
+    s_wcnt[w][d] = tile_count;
+    tile_count += c;
+  }
+
+  // Decoupled look-back for this digit.
+  uint32_t excl = 0;
+  if (tile == 0) {
+    st_volatile(&lookback[d], kLbInclusive | tile_count);
+  } else {
+    st_volatile(&lookback[(size_t)tile * kRadix + d], kLbAggregate | tile_count);
+    int t = (int)tile - 1;
+    uint32_t spins = 0;
+    while (true) {
+      const uint32_t v = ld_volatile(&lookback[(size_t)t * kRadix + d]);
+      const uint32_t flag = v & ~kLbMask;
+      if (flag == 0u) {
+        if (++spins >= kSpinLimit) {
+          atomicOr(err, kDevErrLookback);
+          break;
+        }
+        if (spins > 64) __nanosleep(32);
+        continue;
+      }
+      excl += v & kLbMask;
+      if (flag == kLbInclusive || t == 0) break;
+      --t;
+    }
+    st_volatile(&lookback[(size_t)tile * kRadix + d],
+                kLbInclusive | ((excl + tile_count) & kLbMask));
+  }
+  s_gbase[d] = global_excl[d] + excl;
+  s_dexcl[d] = block_exclusive_scan(tile_count, s_warp);
+  __syncthreads();
+
+  // Stage the tile in digit order in shared memory, then write it out with
+  // consecutive threads on consecutive destinations.
+#pragma unroll
+  for (int it = 0; it < kSortItems; ++it) {
+    const uint32_t idx = seg + (uint32_t)it * 32u + lane;
+    if (idx < n) {
+      const uint32_t dg = (key[it] >> shift) & (kRadix - 1);
+      const uint32_t lp = s_dexcl[dg] + s_wcnt[warp][dg] + rank[it];
+      s_keys[lp] = key[it];
+      s_vals[lp] = val[it];
+    }
+  }
+  __syncthreads();
+  const uint32_t tile_n = min((uint32_t)kSortTile, n - tile_base);
+  for (uint32_t i = tid; i < tile_n; i += kSortThreads) {
+    const uint32_t k = s_keys[i];
+    const uint32_t dg = (k >> shift) & (kRadix - 1);
+    const uint32_t dst = s_gbase[dg] + (i - s_dexcl[dg]);
+    // Always true unless a look-back wait gave up (error flag set).
+    if (dst < n) {
+      keys_out[dst] = k;
+      vals_out[dst] = s_vals[i];
+    }
+  }
+}
+
+__global__ void k_cell_offsets(const uint32_t *__restrict__ skeys, uint32_t n,
+                               uint32_t ncells, uint32_t *__restrict__ off) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const uint32_t k = min(skeys[q], ncells);
+  const uint32_t first = q ? min(skeys[q - 1], ncells) + 1u : 0u;
+  for (uint32_t c = first; c <= k && c < ncells; ++c) off[c] = q;
+  if (q == n - 1)
+    for (uint32_t c = k + 1u; c <= ncells; ++c) off[c] = n;
+}
+
+__global__ void k_find_cells(const uint32_t *__restrict__ off, uint32_t ncells,
+                             int2 *__restrict__ out) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const uint32_t a = off[c], b = off[c + 1];
+  out[c] = a < b ? make_int2((int)a, (int)(b - 1)) : make_int2(-1, -1);
+}
+
+__global__ void k_cell_hash(const float4 *__restrict__ pred, uint32_t n,
+                            SceneDesc scene, uint32_t *__restrict__ hash) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p = pred[i];
+  hash[i] = scene.cell_base + scene_cell(p.x, p.y, p.z, scene);
+}
+
+inline uint32_t blocks_for(uint64_t n, uint32_t t) {
+  return (uint32_t)((n + t - 1) / t);
+}
+
+}  // namespace
+
+uint32_t bits_for(uint32_t max_key_exclusive) {
+  uint32_t b = 1;
+  while (b < 32 && (1ull << b) < (uint64_t)max_key_exclusive) ++b;
+  return b;
+}
+
+SortPlan make_sort_plan(uint32_t n, uint32_t key_bits) {
+  SortPlan p;
+  p.n = n;
+  p.key_bits = key_bits < 1 ? 1 : (key_bits > 32 ? 32 : key_bits);
+  p.passes = (p.key_bits + kRadixBits - 1) / kRadixBits;
+  p.tiles = (uint32_t)(((uint64_t)n + kSortTile - 1) / kSortTile);
+  size_t w = 0;
+  p.off_hist = w;
+  w += (size_t)p.passes * kRadix;
+  p.off_counter = w;
+  w += 32;
+  p.off_lookback = w;
+  w += (size_t)p.passes * p.tiles * kRadix;
+  p.clear_words = w - p.off_hist;
+  w = (w + 63) & ~size_t(63);
+  p.off_keys_alt = w;
+  w += (size_t)n;
+  w = (w + 63) & ~size_t(63);
+  p.off_vals_alt = w;
+  w += (size_t)n;
+  p.words = w;
+  return p;
+}
+
+uint32_t sort_pass_launches(const SortPlan &plan) { return 2u + plan.passes; }
+
+cudaError_t sort_clear(const SortPlan &plan, uint32_t *scratch,
+                       cudaStream_t stream) {
+  return cudaMemsetAsync(scratch + plan.off_hist, 0,
+                         plan.clear_words * sizeof(uint32_t), stream);
+}
+
+cudaError_t sort_histogram(const SortPlan &plan, const uint32_t *keys,
+                           uint32_t *scratch, cudaStream_t stream) {
+  if (plan.n == 0) return cudaSuccess;
+  const uint32_t blocks = min(blocks_for(plan.n, 256), 152u * 8u);
+  k_sort_histogram<<<blocks, 256, 0, stream>>>(keys, plan.n, plan.passes,
+                                               scratch + plan.off_hist);
+  return cudaGetLastError();
+}
+
+cudaError_t sort_scan(const SortPlan &plan, uint32_t *scratch,
+                      cudaStream_t stream) {
+  k_sort_scan<<<1, kSortThreads, 0, stream>>>(plan.passes,
+                                              scratch + plan.off_hist);
+  return cudaGetLastError();
+}
+
+cudaError_t sort_passes(const SortPlan &plan, const uint32_t *keys_in,
+                        const uint32_t *vals_in, uint32_t *keys_out,
+                        uint32_t *vals_out, uint32_t *scratch, uint32_t *err,
+                        cudaStream_t stream) {
+  if (plan.n == 0) return cudaSuccess;
+  uint32_t *kalt = scratch + plan.off_keys_alt;
+  uint32_t *valt = scratch + plan.off_vals_alt;
+  // Arrange the ping-pong so the last pass writes keys_out/vals_out and the
+  // inputs are never written.
+  const uint32_t *ksrc = keys_in;
+  const uint32_t *vsrc = vals_in;
+  for (uint32_t p = 0; p < plan.passes; ++p) {
+    const bool to_out = ((plan.passes - 1 - p) % 2) == 0;
+    uint32_t *kdst = to_out ? keys_out : kalt;
+    uint32_t *vdst = to_out ? vals_out : valt;
+    uint32_t *hist = scratch + plan.off_hist + (size_t)p * kRadix;
+    uint32_t *lb = scratch + plan.off_lookback + (size_t)p * plan.tiles * kRadix;
+    uint32_t *ctr = scratch + plan.off_counter + p;
+    if (p == 0 && vsrc == nullptr) {
+      k_onesweep<true><<<plan.tiles, kSortThreads, 0, stream>>>(
+          ksrc, nullptr, kdst, vdst, plan.n, p * kRadixBits, hist, lb, ctr, err);
+    } else {
+      k_onesweep<false><<<plan.tiles, kSortThreads, 0, stream>>>(
+          ksrc, vsrc, kdst, vdst, plan.n, p * kRadixBits, hist, lb, ctr, err);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    ksrc = kdst;
+    vsrc = vdst;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t cell_offsets(const uint32_t *sorted_keys, uint32_t n,
+                         uint32_t ncells, uint32_t *offsets,
+                         cudaStream_t stream) {
+  if (n == 0) return cudaMemsetAsync(offsets, 0, (ncells + 1ull) * 4, stream);
+  k_cell_offsets<<<blocks_for(n, 256), 256, 0, stream>>>(sorted_keys, n, ncells,
+                                                        offsets);
+  return cudaGetLastError();
+}
+
+cudaError_t find_cells(const uint32_t *offsets, uint32_t ncells,
+                       int32_t *first_last, cudaStream_t stream) {
+  if (ncells == 0) return cudaSuccess;
+  k_find_cells<<<blocks_for(ncells, 256), 256, 0, stream>>>(
+      offsets, ncells, reinterpret_cast<int2 *>(first_last));
+  return cudaGetLastError();
+}
+
+cudaError_t cell_hash(const float4 *pred, uint32_t n, const SceneDesc &scene,
+                      uint32_t *hash, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  k_cell_hash<<<blocks_for(n, 256), 256, 0, stream>>>(pred, n, scene, hash);
+  return cudaGetLastError();
+}
+
+}  // namespace pbf

@@ -1,0 +1,126 @@
+"""Synthetic scenes: seeded dam-break blocks with the benchmark shapes.
+
+Every scene uses spacing 0.05 = h/2 with h = 0.1 (so the number density at
+rest is 1/0.05^3 = 8000 per cubic metre: a fluid of 1000 kg/m^3 made of
+particles of mass 1000*0.05^3 = 0.125 kg), gravity -9.81 along y, dt = 1/120,
+4 solver iterations, relaxation epsilon 600, s_corr k = 0.1, n = 4,
+dq = 0.2 h, XSPH c = 0.01 and vorticity epsilon 0.0005.  Each coordinate is
+jittered by U(-0.01 spacing, +0.01 spacing) from the library's splitmix64
+generator (seed 0x5EED unless given).
+
+Block placement: the paper-mode walls sit h/4 inside the box, so a lattice
+whose first particle is h/4 from the wall and whose extent is a whole number
+of spacings fills the span between opposite walls exactly.  Blocks start at
+the box minimum plus h/4 on every axis.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import MODE_PAPER, PARTICLE_DTYPE, Params, default_params, generate_block
+
+H = 0.1
+SPACING = 0.05
+MASS = 1000.0 * SPACING ** 3
+REST_DENSITY = 1.0 / SPACING ** 3
+JITTER = 0.01 * SPACING
+SEED = 0x5EED
+DT = 1.0 / 120.0
+
+
+@dataclass
+class Scene:
+    name: str
+    params: Params
+    particles: np.ndarray
+    steps: int
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return int(self.particles.shape[0])
+
+
+def base_params(box, cells, mode: int = MODE_PAPER) -> Params:
+    p = default_params(mode)
+    (p.x_min, p.y_min, p.z_min), (p.x_max, p.y_max, p.z_max) = (0.0, 0.0, 0.0), box
+    p.x_n, p.y_n, p.z_n = cells
+    p.time_step_length = DT
+    p.rest_density = REST_DENSITY
+    p.solver_iterations = 4
+    p.relax_eps = 600.0
+    p.scorr_k = 0.1
+    p.scorr_n = 4
+    p.scorr_dq = 0.2
+    p.xsph_c = 0.01
+    p.vort_eps = 0.0005
+    p.gravity_y = -9.81
+    p.wall_margin = 0.25 * H
+    p.max_neighbours = 64
+    return p
+
+
+def block(origin, dims, seed: int) -> np.ndarray:
+    nx, ny, nz = dims
+    return generate_block(origin, nx, ny, nz, SPACING, JITTER, MASS, seed)
+
+
+def dam_break(dims=(32, 32, 32), box=(1.6, 1.6, 3.2), seed: int = SEED, name: str = "dam_break") -> Scene:
+    """One block in the box's minimum corner; cells of size h."""
+    cells = tuple(int(round(b / H)) for b in box)
+    p = base_params(box, cells)
+    m = 0.25 * H
+    ps = block((m, m, m), dims, seed)
+    return Scene(name, p, ps, 500, {"block": list(dims), "box": list(box), "cells": list(cells),
+                                    "origin": [m, m, m], "seed": seed})
+
+
+def config_small(seed: int = SEED) -> Scene:
+    """32,768 particles (32^3 block) in a 1.6 x 1.6 x 3.2 box, 500 steps."""
+    return dam_break((32, 32, 32), (1.6, 1.6, 3.2), seed, "dam_break_32k")
+
+
+def config_1m(seed: int = SEED) -> Scene:
+    """1,048,576 particles (128 x 128 x 64 block) in a 6.4^3 box, 500 steps."""
+    return dam_break((128, 128, 64), (6.4, 6.4, 6.4), seed, "single_scene_1m")
+
+
+def config_4m(seed: int = SEED) -> Scene:
+    """4,194,304 particles: two 128^3 blocks on the floor at opposite x ends of
+    a 12.8 x 12.8 x 6.4 box, collapsing into each other; 200 steps."""
+    box = (12.8, 12.8, 6.4)
+    cells = (128, 128, 64)
+    p = base_params(box, cells)
+    m = 0.25 * H
+    a = block((m, m, m), (128, 128, 128), seed)
+    bx = box[0] - m - 127 * SPACING
+    b = block((bx, m, m), (128, 128, 128), seed + 1)
+    ps = np.concatenate([a, b])
+    return Scene("double_dam_break_4m", p, ps, 200,
+                 {"blocks": [[128, 128, 128]] * 2, "box": list(box), "cells": list(cells),
+                  "origins": [[m, m, m], [bx, m, m]], "seed": seed})
+
+
+def mixed_batch(count: int = 256, n_min: int = 4096, n_max: int = 262144, seed: int = SEED) -> list[Scene]:
+    """Independent dam breaks with log-uniform particle counts and block
+    aspect ratios in [0.5, 2]; each box is twice the block extent."""
+    rng = np.random.default_rng(seed)
+    scenes = []
+    for s in range(count):
+        n_target = math.exp(rng.uniform(math.log(n_min), math.log(n_max)))
+        ax, az = rng.uniform(0.5, 2.0, size=2)
+        # block dims proportional to (ax, 1, az) with product ~ n_target
+        base = (n_target / (ax * az)) ** (1.0 / 3.0)
+        dims = tuple(max(2, int(round(v))) for v in (base * ax, base, base * az))
+        ext = [(d - 1) * SPACING + 2 * 0.25 * H for d in dims]
+        cells = tuple(max(1, int(math.ceil(2 * e / H))) for e in ext)
+        box = tuple(c * H for c in cells)
+        p = base_params(box, cells)
+        m = 0.25 * H
+        ps = block((m, m, m), dims, seed + 1000 + s)
+        scenes.append(Scene(f"batch_{s}", p, ps, 300, {"block": list(dims), "box": list(box),
+                                                        "cells": list(cells)}))
+    return scenes
