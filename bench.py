@@ -163,7 +163,7 @@ def reduce_max(dist, value: float, device=None) -> float:
     return float(t.item())
 
 
-def cpu_reference_run(n_steps_max: int = 10, budget_s: float = 15.0, threads: int = 0):
+def cpu_reference_run(n_steps_max: int = 50, budget_s: float = 15.0, threads: int = 0):
     """Times the reference's own kernels (or the oracle restatement where
     they are not built) on the 1M workload, one step at a time until
     `budget_s` of CPU time is spent.  Returns (value, info)."""
@@ -348,7 +348,7 @@ def run_ours(args) -> int:
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline work")

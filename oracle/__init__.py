@@ -75,9 +75,9 @@ def restatement():
             cfgp, C.c_uint32, _F32P, _F32P, C.c_uint32, C.c_float, C.c_int, C.c_void_p, C.c_void_p]
         lib.oracle_refcompat_steps_f64.argtypes = [
             cfgp, C.c_uint32, _F64P, _F64P, C.c_uint32, C.c_double, C.c_int]
-        lib.oracle_paper_steps_f64.argtypes = [
-            C.POINTER(PaperParams), C.c_uint32, _F64P, _F64P, C.c_uint32, C.c_double, C.c_int,
-            C.c_void_p, C.c_void_p, C.c_void_p]
+        for fn in (lib.oracle_paper_steps_f64, lib.oracle_paper_steps_f32):
+            fn.argtypes = [C.POINTER(PaperParams), C.c_uint32, _F64P, _F64P, C.c_uint32, C.c_double,
+                           C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib_restatement = lib
     return _lib_restatement
 
@@ -163,17 +163,19 @@ def refcompat_steps_f64(cfg: Config, pos4, vel4, steps: int, wave: float = 0.0, 
     return pos, vel
 
 
-def paper_steps_f64(prm: PaperParams, pos4, vel4, steps: int, wave: float = 0.0, threads: int = 0):
-    """Returns (pos4, vel4, density, lambda, neighbour_count) after `steps`."""
+def paper_steps_f64(prm: PaperParams, pos4, vel4, steps: int, wave: float = 0.0, threads: int = 0,
+                    precision: str = "f64"):
+    """Returns (pos4, vel4, density, lambda, neighbour_count) after `steps`.
+    precision="f32" evaluates the same algorithm in binary32."""
     pos = np.array(pos4, np.float64, copy=True).reshape(-1, 4)
     vel = np.array(vel4, np.float64, copy=True).reshape(-1, 4)
     n = pos.shape[0]
     dens = np.zeros(n, np.float64)
     lam = np.zeros(n, np.float64)
     cnt = np.zeros(n, np.uint32)
-    _check(restatement().oracle_paper_steps_f64(
-        C.byref(prm), n, pos.reshape(-1), vel.reshape(-1), steps, wave, threads,
-        _ptr(dens), _ptr(lam), _ptr(cnt)), "paper_steps_f64")
+    fn = restatement().oracle_paper_steps_f64 if precision == "f64" else restatement().oracle_paper_steps_f32
+    _check(fn(C.byref(prm), n, pos.reshape(-1), vel.reshape(-1), steps, wave, threads,
+              _ptr(dens), _ptr(lam), _ptr(cnt)), "paper_steps")
     return pos, vel, dens, lam, cnt
 
 

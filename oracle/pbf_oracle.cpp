@@ -369,28 +369,29 @@ int refcompat_steps(const oracle_config *cfg, uint32_t n, T *pos4, T *vel4,
  * positions at the start of the step (paper, Algorithm 1 line 6) and every
  * kernel evaluated at the current positions with W = 0 beyond h.  rho_j in
  * the velocity terms is the density of the last lambda pass.            */
+template <typename T>
 struct Paper {
   oracle_paper_params prm;
   uint32_t n = 0;
   int threads = 1;
-  double h, h2, poly6c, spikyc, rho_self, dq2, cl[3];
-  std::vector<double> x, v, m, pw, d, p, lam, rho, dpx, vel, om, omn;
+  T h, h2, poly6c, spikyc, rho_self, dq2, cl[3];
+  std::vector<T> x, v, m, pw, d, p, lam, rho, dpx, vel, om, omn;
   std::vector<uint32_t> nbr_off, nbr;
 
   void setup() {
-    h = prm.h;
+    h = (T)prm.h;
     h2 = h * h;
     poly6c = 315.0 / (64.0 * M_PI * std::pow(h, 9));
     spikyc = 45.0 / (M_PI * std::pow(h, 6));
     rho_self = poly6c * h2 * h2 * h2;
-    const double dq = prm.scorr_dq * h;
+    const T dq = (T)prm.scorr_dq * h;
     dq2 = dq * dq;
     for (int a = 0; a < 3; ++a)
-      cl[a] = (prm.box_max[a] - prm.box_min[a]) / prm.n_cells[a];
+      cl[a] = ((T)prm.box_max[a] - (T)prm.box_min[a]) / (T)prm.n_cells[a];
   }
 
-  int cell_axis(double q, int a) const {
-    int c = (int)std::floor((q - prm.box_min[a]) / cl[a]);
+  int cell_axis(T q, int a) const {
+    int c = (int)std::floor((q - (T)prm.box_min[a]) / cl[a]);
     return c < 0 ? 0 : (c >= prm.n_cells[a] ? prm.n_cells[a] - 1 : c);
   }
 
@@ -424,9 +425,9 @@ struct Paper {
             for (uint32_t q = cnt[c]; q < cnt[c + 1]; ++q) {
               const uint32_t j = order[q];
               if (j == i) continue;
-              const double rx = p[3 * i] - p[3 * j], ry = p[3 * i + 1] - p[3 * j + 1],
+              const T rx = p[3 * i] - p[3 * j], ry = p[3 * i + 1] - p[3 * j + 1],
                            rz = p[3 * i + 2] - p[3 * j + 2];
-              const double r2 = rx * rx + ry * ry + rz * rz;
+              const T r2 = rx * rx + ry * ry + rz * rz;
               if (r2 > 0.0 && r2 < h2) L.push_back(j);
             }
           }
@@ -440,14 +441,14 @@ struct Paper {
   }
 
   /* g_ij and r^2 at the current positions; false if r >= h or r == 0. */
-  bool grad(uint32_t i, uint32_t j, double g[3], double *r2o) const {
-    const double rx = p[3 * i] - p[3 * j], ry = p[3 * i + 1] - p[3 * j + 1],
+  bool grad(uint32_t i, uint32_t j, T g[3], T *r2o) const {
+    const T rx = p[3 * i] - p[3 * j], ry = p[3 * i + 1] - p[3 * j + 1],
                  rz = p[3 * i + 2] - p[3 * j + 2];
-    const double r2 = rx * rx + ry * ry + rz * rz;
+    const T r2 = rx * rx + ry * ry + rz * rz;
     *r2o = r2;
     if (!(r2 > 0.0 && r2 < h2)) return false;
-    const double r = std::sqrt(r2);
-    const double f = -spikyc * (h - r) * (h - r) / r;
+    const T r = std::sqrt(r2);
+    const T f = -spikyc * (h - r) * (h - r) / r;
     g[0] = f * rx;
     g[1] = f * ry;
     g[2] = f * rz;
@@ -458,49 +459,56 @@ struct Paper {
 #pragma omp parallel for num_threads(threads) schedule(dynamic, 256)
     for (long li = 0; li < (long)n; ++li) {
       const uint32_t i = (uint32_t)li;
-      double dens = rho_self, G[3] = {0, 0, 0}, S = 0;
+      // Density summed with a compensation term (Fast2Sum: the running sum
+      // starts at W(0), the largest term), so that C = rho/rho0 - 1, a small
+      // difference of large numbers, keeps its precision.
+      T dens = rho_self, dens_lo = 0, G[3] = {0, 0, 0}, S = 0;
       for (uint32_t q = nbr_off[i]; q < nbr_off[i + 1]; ++q) {
         const uint32_t j = nbr[q];
-        double g[3], r2;
+        T g[3], r2;
         if (!grad(i, j, g, &r2)) continue;
-        const double t = h2 - r2;
-        dens += poly6c * t * t * t;
+        const T t = h2 - r2;
+        const T w = poly6c * t * t * t;
+        const T sum = dens + w;
+        dens_lo += w - (sum - dens);
+        dens = sum;
         G[0] += g[0];
         G[1] += g[1];
         G[2] += g[2];
         S += g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
       }
-      const double rho0 = prm.rest_density;
-      const double C = dens / rho0 - 1.0;
-      const double den = (G[0] * G[0] + G[1] * G[1] + G[2] * G[2] + S) / (rho0 * rho0);
-      lam[i] = -C / (den + prm.relax_eps);
+      const T rho0 = (T)prm.rest_density;
+      const T C = ((dens - rho0) + dens_lo) / rho0;
+      dens += dens_lo;
+      const T den = (G[0] * G[0] + G[1] * G[1] + G[2] * G[2] + S) / (rho0 * rho0);
+      lam[i] = -C / (den + (T)prm.relax_eps);
       rho[i] = dens;
     }
   }
 
-  void delta_pass(double wave) {
-    const double dn = (h2 - dq2);
+  void delta_pass(T wave) {
+    const T dn = (h2 - dq2);
     const int sn = prm.scorr_n;
 #pragma omp parallel for num_threads(threads) schedule(dynamic, 256)
     for (long li = 0; li < (long)n; ++li) {
       const uint32_t i = (uint32_t)li;
-      double s[3] = {0, 0, 0};
+      T s[3] = {0, 0, 0};
       for (uint32_t q = nbr_off[i]; q < nbr_off[i + 1]; ++q) {
         const uint32_t j = nbr[q];
-        double g[3], r2;
+        T g[3], r2;
         if (!grad(i, j, g, &r2)) continue;
-        const double ratio = std::pow((h2 - r2) / dn, 3.0 * sn);
-        const double sc = -prm.scorr_k * h2 * ratio;
-        const double w = lam[i] + lam[j] + sc;
+        const T ratio = std::pow((h2 - r2) / dn, 3.0 * sn);
+        const T sc = -(T)prm.scorr_k * h2 * ratio;
+        const T w = lam[i] + lam[j] + sc;
         s[0] += w * g[0];
         s[1] += w * g[1];
         s[2] += w * g[2];
       }
       for (int a = 0; a < 3; ++a) {
-        const double dnew = d[3 * i + a] + s[a] / prm.rest_density;
-        double q = x[3 * i + a] + dnew;
-        double lo = prm.box_min[a] + prm.wall_margin + (a == 0 ? wave : 0.0);
-        double hi = prm.box_max[a] - prm.wall_margin;
+        const T dnew = d[3 * i + a] + s[a] / (T)prm.rest_density;
+        T q = x[3 * i + a] + dnew;
+        const T lo = (T)(prm.box_min[a] + prm.wall_margin) + (a == 0 ? (T)wave : (T)0);
+        const T hi = (T)(prm.box_max[a] - prm.wall_margin);
         if (q < lo) q = lo;
         else if (q > hi) q = hi;
         dpx[3 * i + a] = q - x[3 * i + a];
@@ -511,18 +519,18 @@ struct Paper {
   }
 
   void velocity_pass() {
-    const double dt = prm.dt;
+    const T dt = (T)prm.dt;
     for (size_t q = 0; q < (size_t)3 * n; ++q) vel[q] = d[q] / dt;
 #pragma omp parallel for num_threads(threads) schedule(dynamic, 256)
     for (long li = 0; li < (long)n; ++li) {
       const uint32_t i = (uint32_t)li;
-      double w[3] = {0, 0, 0};
+      T w[3] = {0, 0, 0};
       for (uint32_t q = nbr_off[i]; q < nbr_off[i + 1]; ++q) {
         const uint32_t j = nbr[q];
-        double g[3], r2;
+        T g[3], r2;
         if (!grad(i, j, g, &r2)) continue;
-        const double vj = 1.0 / rho[j];
-        const double u[3] = {vel[3 * j] - vel[3 * i], vel[3 * j + 1] - vel[3 * i + 1],
+        const T vj = 1.0 / rho[j];
+        const T u[3] = {vel[3 * j] - vel[3 * i], vel[3 * j + 1] - vel[3 * i + 1],
                              vel[3 * j + 2] - vel[3 * i + 2]};
         w[0] += vj * (g[1] * u[2] - g[2] * u[1]);
         w[1] += vj * (g[2] * u[0] - g[0] * u[2]);
@@ -536,42 +544,43 @@ struct Paper {
 #pragma omp parallel for num_threads(threads) schedule(dynamic, 256)
     for (long li = 0; li < (long)n; ++li) {
       const uint32_t i = (uint32_t)li;
-      double eta[3] = {0, 0, 0}, xs[3] = {0, 0, 0};
+      T eta[3] = {0, 0, 0}, xs[3] = {0, 0, 0};
       for (uint32_t q = nbr_off[i]; q < nbr_off[i + 1]; ++q) {
         const uint32_t j = nbr[q];
-        double g[3], r2;
+        T g[3], r2;
         if (!grad(i, j, g, &r2)) continue;
-        const double vj = 1.0 / rho[j];
-        const double dw = vj * (omn[j] - omn[i]);
+        const T vj = 1.0 / rho[j];
+        const T dw = vj * (omn[j] - omn[i]);
         eta[0] += dw * g[0];
         eta[1] += dw * g[1];
         eta[2] += dw * g[2];
-        const double t = h2 - r2;
-        const double W = poly6c * t * t * t * vj;
+        const T t = h2 - r2;
+        const T W = poly6c * t * t * t * vj;
         xs[0] += W * (vel[3 * j] - vel[3 * i]);
         xs[1] += W * (vel[3 * j + 1] - vel[3 * i + 1]);
         xs[2] += W * (vel[3 * j + 2] - vel[3 * i + 2]);
       }
-      const double el = std::sqrt(eta[0] * eta[0] + eta[1] * eta[1] + eta[2] * eta[2]);
-      double N[3] = {0, 0, 0};
+      const T el = std::sqrt(eta[0] * eta[0] + eta[1] * eta[1] + eta[2] * eta[2]);
+      T N[3] = {0, 0, 0};
       if (el > 0.0) {
         N[0] = eta[0] / el;
         N[1] = eta[1] / el;
         N[2] = eta[2] / el;
       }
-      const double *o = &om[3 * i];
-      const double f[3] = {prm.vort_eps * (N[1] * o[2] - N[2] * o[1]),
-                           prm.vort_eps * (N[2] * o[0] - N[0] * o[2]),
-                           prm.vort_eps * (N[0] * o[1] - N[1] * o[0])};
+      const T *o = &om[3 * i];
+      const T ve = (T)prm.vort_eps, dt = (T)prm.dt, c = (T)prm.xsph_c;
+      const T f[3] = {ve * (N[1] * o[2] - N[2] * o[1]),
+                      ve * (N[2] * o[0] - N[0] * o[2]),
+                      ve * (N[0] * o[1] - N[1] * o[0])};
       for (int a = 0; a < 3; ++a)
-        dpx[3 * i + a] = vel[3 * i + a] + prm.dt * f[a] + prm.xsph_c * xs[a];
+        dpx[3 * i + a] = vel[3 * i + a] + dt * f[a] + c * xs[a];
     }
   }
 
-  void step(double wave) {
-    const double dt = prm.dt;
+  void step(T wave) {
+    const T dt = (T)prm.dt;
     for (uint32_t i = 0; i < n; ++i) {
-      v[3 * i + 1] += dt * prm.gravity_y;
+      v[3 * i + 1] += dt * (T)prm.gravity_y;
       for (int a = 0; a < 3; ++a) {
         d[3 * i + a] = dt * v[3 * i + a];
         p[3 * i + a] = x[3 * i + a] + d[3 * i + a];
@@ -584,7 +593,7 @@ struct Paper {
     }
     velocity_pass();
     for (uint32_t i = 0; i < n; ++i) {
-      double s2 = 0;
+      T s2 = 0;
       for (int a = 0; a < 3; ++a) {
         x[3 * i + a] = p[3 * i + a];
         v[3 * i + a] = dpx[3 * i + a];
@@ -668,17 +677,22 @@ int oracle_refcompat_steps_f64(const oracle_config *cfg, uint32_t n,
                                  nullptr, nullptr);
 }
 
-int oracle_paper_steps_f64(const oracle_paper_params *prm, uint32_t n,
-                           double *pos4, double *vel4, uint32_t steps,
-                           double wave, int threads, double *density_out,
-                           double *lambda_out, uint32_t *nbr_count_out) {
+}  // extern "C"
+
+namespace {
+
+template <typename T>
+int paper_steps(const oracle_paper_params *prm, uint32_t n, double *pos4,
+                double *vel4, uint32_t steps, double wave, int threads,
+                double *density_out, double *lambda_out,
+                uint32_t *nbr_count_out) {
   if (!prm || !pos4 || !vel4 || n == 0) return 1;
   for (int a = 0; a < 3; ++a)
     if (prm->n_cells[a] < 1 || !(prm->box_max[a] > prm->box_min[a])) return 1;
   if (!(prm->h > 0) || !(prm->dt > 0) || !(prm->rest_density > 0) ||
       prm->iterations < 0)
     return 1;
-  Paper s;
+  Paper<T> s;
   s.prm = *prm;
   s.n = n;
   s.threads = threads > 0 ? threads : omp_get_max_threads();
@@ -703,7 +717,7 @@ int oracle_paper_steps_f64(const oracle_paper_params *prm, uint32_t n,
     s.pw[i] = pos4[4 * i + 3];
     s.m[i] = vel4[4 * i + 3];
   }
-  for (uint32_t t = 0; t < steps; ++t) s.step(wave);
+  for (uint32_t t = 0; t < steps; ++t) s.step((T)wave);
   for (uint32_t i = 0; i < n; ++i) {
     for (int a = 0; a < 3; ++a) {
       pos4[4 * i + a] = s.x[3 * i + a];
@@ -716,6 +730,26 @@ int oracle_paper_steps_f64(const oracle_paper_params *prm, uint32_t n,
     if (nbr_count_out) nbr_count_out[i] = s.nbr_off[i + 1] - s.nbr_off[i];
   }
   return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_paper_steps_f64(const oracle_paper_params *prm, uint32_t n,
+                           double *pos4, double *vel4, uint32_t steps,
+                           double wave, int threads, double *density_out,
+                           double *lambda_out, uint32_t *nbr_count_out) {
+  return paper_steps<double>(prm, n, pos4, vel4, steps, wave, threads,
+                             density_out, lambda_out, nbr_count_out);
+}
+
+int oracle_paper_steps_f32(const oracle_paper_params *prm, uint32_t n,
+                           double *pos4, double *vel4, uint32_t steps,
+                           double wave, int threads, double *density_out,
+                           double *lambda_out, uint32_t *nbr_count_out) {
+  return paper_steps<float>(prm, n, pos4, vel4, steps, wave, threads,
+                            density_out, lambda_out, nbr_count_out);
 }
 
 }  // extern "C"

@@ -87,6 +87,12 @@ int oracle_paper_steps_f64(const oracle_paper_params *p, uint32_t n,
                            double *pos4, double *vel4, uint32_t steps,
                            double wave, int threads, double *density_out,
                            double *lambda_out, uint32_t *nbr_count_out);
+/* The same algorithm evaluated in float (IEEE, no contraction), for
+ * measuring how far binary32 arithmetic alone moves the result. */
+int oracle_paper_steps_f32(const oracle_paper_params *p, uint32_t n,
+                           double *pos4, double *vel4, uint32_t steps,
+                           double wave, int threads, double *density_out,
+                           double *lambda_out, uint32_t *nbr_count_out);
 
 #ifdef __cplusplus
 }

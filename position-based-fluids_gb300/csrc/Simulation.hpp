@@ -14,7 +14,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/pbf.h"
+#include "pbf.h"
 
 namespace pbf {
 

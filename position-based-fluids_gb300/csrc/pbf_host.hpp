@@ -5,7 +5,7 @@
 
 #include <string>
 
-#include "../../include/pbf.h"
+#include "pbf.h"
 #include "pbf_internal.cuh"
 
 namespace pbf {
