@@ -73,9 +73,9 @@ def measured_peaks() -> dict:
 
 def profile_traffic(kernel: str):
     """dram read+write bytes per launch and particles per launch of `kernel`
-    from the committed ncu summary (profiles/*traffic*.txt lines of the form
+    from the committed ncu summaries (profiles/*.md or *.txt lines of the form
     `traffic kernel=<name> bytes_per_launch=<B> particles=<N>`), or None."""
-    for f in sorted((ROOT / "profiles").glob("*.txt")):
+    for f in sorted([*(ROOT / "profiles").glob("*.txt"), *(ROOT / "profiles").glob("*.md")]):
         for line in f.read_text().splitlines():
             if line.startswith("traffic ") and f"kernel={kernel} " in line + " ":
                 kv = dict(t.split("=", 1) for t in line.split()[1:] if "=" in t)

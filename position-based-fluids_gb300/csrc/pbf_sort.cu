@@ -215,15 +215,20 @@ __global__ void __launch_bounds__(kSortThreads)
   }
 }
 
+// off[c] = number of sorted keys < c, for c in [0, ncells]: one thread per
+// cell, binary search over the sorted keys.  Neighbouring cells search
+// neighbouring key ranges, so the probes of a warp share cache lines.
 __global__ void k_cell_offsets(const uint32_t *__restrict__ skeys, uint32_t n,
                                uint32_t ncells, uint32_t *__restrict__ off) {
-  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n) return;
-  const uint32_t k = min(skeys[q], ncells);
-  const uint32_t first = q ? min(skeys[q - 1], ncells) + 1u : 0u;
-  for (uint32_t c = first; c <= k && c < ncells; ++c) off[c] = q;
-  if (q == n - 1)
-    for (uint32_t c = k + 1u; c <= ncells; ++c) off[c] = n;
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c > ncells) return;
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = lo + ((hi - lo) >> 1);
+    if (__ldg(&skeys[mid]) < c) lo = mid + 1;
+    else hi = mid;
+  }
+  off[c] = lo;
 }
 
 __global__ void k_find_cells(const uint32_t *__restrict__ off, uint32_t ncells,
@@ -339,8 +344,8 @@ cudaError_t cell_offsets(const uint32_t *sorted_keys, uint32_t n,
                          uint32_t ncells, uint32_t *offsets,
                          cudaStream_t stream) {
   if (n == 0) return cudaMemsetAsync(offsets, 0, (ncells + 1ull) * 4, stream);
-  k_cell_offsets<<<blocks_for(n, 256), 256, 0, stream>>>(sorted_keys, n, ncells,
-                                                        offsets);
+  k_cell_offsets<<<blocks_for(ncells + 1ull, 256), 256, 0, stream>>>(
+      sorted_keys, n, ncells, offsets);
   return cudaGetLastError();
 }
 
