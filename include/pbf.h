@@ -238,6 +238,22 @@ int pbf_op_sort_pairs(const uint32_t *d_keys_in, const uint32_t *d_vals_in,
  * give up (its output is then void). */
 int pbf_op_sort_status(const void *d_scratch, uint32_t n, uint32_t key_bits,
                        void *stream);
+/* pbf_op_sort_pairs without any device allocation, for callers that cannot
+ * allocate (a host engine whose own pool owns all device memory, or a
+ * per-frame callback where cudaMalloc/cudaFree would synchronise the device).
+ * No counterpart in the reference.  Scratch is a file-scope device array
+ * sized for at most 1048576 keys (about 9.4 MB on every GPU that loads the
+ * library, held until exit); larger n returns PBF_ERR_INVALID.  The first
+ * call on a device looks the array's address up (cudaGetSymbolAddress), so
+ * make that first call before any stream capture.  All calls share the
+ * array: calls whose work overlaps on the GPU race.  If d_status is not
+ * NULL, look-back failures are OR-ed into *d_status (zeroed by the caller);
+ * otherwise they are not reported. */
+int pbf_op_sort_pairs_noalloc(const uint32_t *d_keys_in,
+                              const uint32_t *d_vals_in, uint32_t n,
+                              uint32_t key_bits, uint32_t *d_keys_out,
+                              uint32_t *d_vals_out, uint32_t *d_status,
+                              void *stream);
 /* CSR cell offsets of sorted keys: d_offsets[c] = number of keys < c for
  * c in [0, ncells]; every key must be < ncells. */
 int pbf_op_cell_offsets(const uint32_t *d_sorted_keys, uint32_t n,

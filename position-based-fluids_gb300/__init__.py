@@ -152,6 +152,7 @@ def lib():
             "pbf_op_sort_scratch_bytes": ([u32, u32], C.c_size_t),
             "pbf_op_sort_pairs": ([vp, vp, u32, u32, vp, vp, vp, C.c_size_t, vp], i32),
             "pbf_op_sort_status": ([vp, u32, u32, vp], i32),
+            "pbf_op_sort_pairs_noalloc": ([vp, vp, u32, u32, vp, vp, vp, vp], i32),
             "pbf_op_cell_offsets": ([vp, u32, u32, vp, vp], i32),
             "pbf_op_find_cells": ([vp, u32, vp, vp], i32),
         }

@@ -1,0 +1,95 @@
+// Radix sort of (key, value) pairs for callers that cannot allocate device
+// memory -- for example a host engine that owns every device allocation
+// through its own pool, or a per-frame callback where cudaMalloc/cudaFree
+// would synchronise the device and stall the frame.  Same sort as
+// pbf_op_sort_pairs; its scratch is a file-scope device array instead of a
+// caller buffer.
+//
+// The array holds the scratch for up to kNoAllocMaxKeys keys
+// (words_for(kNoAllocMaxKeys) 32-bit words, about 9.4 MB).  Every GPU that
+// loads this library keeps it until the process exits.  All calls share it
+// and it keeps the last call's contents: each call first zeroes the
+// histogram, tile-counter and look-back words it relies on, in stream order.
+// Calls whose work overlaps on the GPU (different streams, or different host
+// threads without ordering) race on the array.
+#include <mutex>
+
+#include "pbf_device.cuh"
+#include "pbf_host.hpp"
+
+namespace pbf {
+namespace {
+
+constexpr uint32_t kNoAllocMaxKeys = 1u << 20;
+constexpr int kMaxDevices = 64;
+
+constexpr size_t align64(size_t w) { return (w + 63) & ~size_t(63); }
+// Words make_sort_plan lays out for n keys and the maximum number of passes.
+constexpr size_t words_for(uint32_t n) {
+  const size_t tiles = ((size_t)n + kSortTile - 1) / kSortTile;
+  size_t w = (size_t)kMaxSortPasses * kRadix + 32 +
+             (size_t)kMaxSortPasses * tiles * kRadix;
+  w = align64(w) + n;
+  w = align64(w) + n;
+  return w;
+}
+constexpr size_t kNoAllocWords = words_for(kNoAllocMaxKeys);
+
+static __device__ __align__(256) uint32_t g_sort_scratch[kNoAllocWords];
+
+std::mutex g_mutex;
+void *g_scratch_address[kMaxDevices] = {};
+
+// Device address of g_sort_scratch on the current device, looked up once
+// per device (the host-side name is only a stand-in for it).
+int scratch_address(uint32_t **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_error_message("device ordinal beyond the no-alloc sort's table");
+    return PBF_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (!g_scratch_address[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_sort_scratch);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress");
+    g_scratch_address[dev] = p;
+  }
+  *out = static_cast<uint32_t *>(g_scratch_address[dev]);
+  return PBF_OK;
+}
+
+}  // namespace
+}  // namespace pbf
+
+extern "C" int pbf_op_sort_pairs_noalloc(const uint32_t *d_keys_in,
+                                         const uint32_t *d_vals_in, uint32_t n,
+                                         uint32_t key_bits,
+                                         uint32_t *d_keys_out,
+                                         uint32_t *d_vals_out,
+                                         uint32_t *d_status, void *stream) {
+  using namespace pbf;
+  if (n == 0) return PBF_OK;
+  if (!d_keys_in || !d_keys_out || !d_vals_out) return PBF_ERR_INVALID;
+  if (key_bits < 1 || key_bits > 32) return PBF_ERR_INVALID;
+  if (n > kNoAllocMaxKeys) {
+    set_error_message("pbf_op_sort_pairs_noalloc sorts at most 1048576 keys");
+    return PBF_ERR_INVALID;
+  }
+  const SortPlan plan = make_sort_plan(n, key_bits);
+  if (plan.words > kNoAllocWords) return PBF_ERR_INVALID;
+  uint32_t *scratch = nullptr;
+  const int rc = scratch_address(&scratch);
+  if (rc != PBF_OK) return rc;
+  uint32_t *err = d_status ? d_status : scratch + plan.off_counter + 31;
+  const cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = sort_clear(plan, scratch, st);
+  if (e == cudaSuccess) e = sort_histogram(plan, d_keys_in, scratch, st);
+  if (e == cudaSuccess) e = sort_scan(plan, scratch, st);
+  if (e == cudaSuccess)
+    e = sort_passes(plan, d_keys_in, d_vals_in, d_keys_out, d_vals_out, scratch,
+                    err, st);
+  return cuda_status(e, "pbf_op_sort_pairs_noalloc");
+}
