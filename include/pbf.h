@@ -18,7 +18,8 @@
  * Conventions
  *  - Every function returns an int status (pbf_status); no exception crosses
  *    the boundary.  The reference throws cl::Error / std::runtime_error
- *    (src/hesp.hpp:33, src/io/*.cpp) and its main() exits on them
+ *    (src/hesp.hpp:33, src/io/ConfigReader.cpp, src/io/PartReader.cpp) and
+ *    its main() exits on them
  *    (src/main.cpp:180-186).
  *  - Host arrays of particle state use the reference's dumpData layout
  *    (src/Simulation.cpp:578-591, 120-134): N float4 positions with

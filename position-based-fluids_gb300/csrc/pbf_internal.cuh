@@ -14,6 +14,7 @@ namespace pbf {
 // host reads back at synchronisation points.
 enum DeviceError : uint32_t {
   kDevErrLookback = 1u,  // a radix-sort look-back wait hit its bound
+  kDevErrStaging = 2u,   // a shared-memory staging wait hit its bound
 };
 
 // ------------------------------------------------------------ grid / scene --
@@ -43,6 +44,7 @@ struct PaperConsts {
   int32_t scorr_n3;              // 3 * n
   float xsph_c, vort_eps;
   uint32_t n, maxn;
+  uint32_t tiles;  // cell-block tiles of the gather passes (all scenes)
 };
 
 // The 18 constants the reference bakes into its OpenCL program
@@ -122,7 +124,8 @@ struct DeviceState {
   float *S = nullptr;                  // lambda (ref-compat)
   uint32_t *keys = nullptr, *skeys = nullptr, *perm = nullptr;
   uint32_t *offsets = nullptr;         // ncells + 1
-  uint32_t *nbr = nullptr, *nbr_cnt = nullptr; // neighbour lists (paper)
+  uint4 *nbr = nullptr;                // neighbour lists, 8 x u16 per word (paper)
+  uint32_t *nbr_cnt = nullptr;         // neighbour counts (paper)
   uint32_t *sort_scratch = nullptr;
   uint32_t *err = nullptr;             // device error flag word
   SceneDesc *scenes = nullptr;         // device scene table (1 entry)
@@ -130,6 +133,11 @@ struct DeviceState {
 };
 
 // ------------------------------------------------------- paper-mode launches
+// Raises the dynamic shared-memory limit of the gather kernels (once per
+// process and device, before the first launch).
+cudaError_t paper_configure();
+// Tiles (CTAs) of the gather passes for n particles.
+uint32_t paper_tiles(uint32_t n);
 cudaError_t paper_predict_hash(const float4 *X, const float4 *V, uint32_t n,
                                const PaperConsts &c, const SceneDesc *scenes,
                                const uint16_t *sid, uint32_t *keys,

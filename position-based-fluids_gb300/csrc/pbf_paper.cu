@@ -14,27 +14,49 @@
 //   X2, V2  state at the start of the step, V2 with gravity applied
 //   P       predicted position x + d
 //   D       displacement d since the start of the step (kept apart from x so
-//           that positions round once per step, not once per iteration)
+//           that positions round once per step, not once per iteration);
+//           after the last delta-p pass it holds (p, |vorticity|)
 //   Q       (predicted position, lambda) as read by the delta-p pass
 //   U       (velocity, 1/rho) as read by the velocity passes
 //   W       (vorticity, |vorticity|)
-//   nbr     neighbour lists, slot-major: nbr[s*N + k]
 // Neighbour sets are built once per step from the predicted positions
 // (Algorithm 1 line 6): N_k = { j != k : 0 < |p_k - p_j| < h } over the 27
 // cells around k's cell.  Every later pass evaluates the kernels at the
-// current positions with W = 0 beyond h.  A particle whose set exceeds the
-// list capacity keeps the true count, and every pass re-derives its set
-// from the cells and the step-start positions instead of the list.
+// current positions with W = 0 beyond h.
+//
+// Gather passes work on tiles of kTile consecutive sorted particles, one
+// thread each.  Sorted by cell key, a tile's particles sit in one or two
+// x-rows of the grid; the 27-cell neighbourhoods of each row's share lie in
+// 9 row ranges (the share's x span widened by one cell, in the rows y-1..y+1,
+// z-1..z+1), which are contiguous slot ranges of the sorted arrays: 18
+// ranges at most.  Neighbour lists store each neighbour as 16 bits, the
+// range (5 bits) and the offset inside it (11 bits), eight per 16-byte word:
+// group g of particle k is nbr4[g*N + k], so a warp reads its particles' next
+// eight neighbours with one coalesced load per thread, and the eight
+// neighbour loads that follow are independent.  A tile spanning more than
+// two rows (sparse regions) or two scenes, a range longer than 2048 slots,
+// and a particle whose set exceeds the list capacity re-derive the set from
+// the cells and the step-start positions in every pass instead (same order,
+// same arithmetic).
+//
+// The neighbour data itself is gathered through L1: measured on GB300, a
+// variant that first staged each tile's ranges into shared memory with
+// cp.async.bulk (mbarrier completion) ran 1.1-2x slower per pass than these
+// L1 gathers -- the copy latency serialises with the compute of a tile and
+// the staging buffers cap occupancy, while L1 already serves ~70% of the
+// neighbour reads.
 #include "pbf_device.cuh"
 
 namespace pbf {
 
 namespace {
 
-constexpr int kGatherThreads = 128;
+constexpr int kTile = 128;          // particles (threads) per gather CTA
+constexpr uint32_t kRelBits = 11;   // offset bits of a list entry
+constexpr uint32_t kRelMax = 1u << kRelBits;
 
 struct NbrCtx {
-  const uint32_t *__restrict__ nbr;
+  const uint4 *__restrict__ nbr4;
   const uint32_t *__restrict__ cnt;
   const uint32_t *__restrict__ skeys;
   const uint32_t *__restrict__ off;
@@ -42,8 +64,18 @@ struct NbrCtx {
   const float4 *__restrict__ V2;
   const SceneDesc *__restrict__ scenes;
   const uint16_t *__restrict__ sid;
+  uint32_t *err;
   uint32_t n, maxn;
   float dt, h2;
+};
+
+// Per-CTA description of the tile's neighbourhood ranges.
+struct Ranges {
+  uint32_t S[32];    // first slot of each row range (18 used)
+  uint32_t len[32];  // slots in each row range
+  uint32_t row_a, nparts, xa[2], xb[2];
+  uint32_t listed;   // 1: lists encode this tile's neighbours; 0: fallback
+  uint32_t scene;
 };
 
 __device__ __forceinline__ const SceneDesc &scene_of(const SceneDesc *scenes,
@@ -52,20 +84,120 @@ __device__ __forceinline__ const SceneDesc &scene_of(const SceneDesc *scenes,
   return scenes[sid ? sid[k] : 0];
 }
 
+__host__ __device__ __forceinline__ uint32_t gather_tiles(uint32_t n) {
+  return (n + kTile - 1) / kTile;
+}
+
+// Computes the row ranges of tile `tile` (particles [tile*kTile, +kTile)):
+// range 9*part + (dz+1)*3 + (dy+1) covers, in row (y+dy, z+dz), the cells
+// x in [xa-1, xb+1] clipped to the row, where part 0/1 is the tile's first/
+// second row and [xa, xb] the x span of its particles there.  Every pass of
+// a step computes the same result (it depends only on the sort).  Returns
+// false, uniformly, for a tile past the end.
+__device__ __forceinline__ bool ranges_setup(Ranges &w, uint32_t tile, const NbrCtx &c) {
+  const uint32_t k0 = tile * (uint32_t)kTile;
+  if (k0 >= c.n) return false;
+  const uint32_t k1 = min(k0 + (uint32_t)kTile, c.n) - 1u;
+  if (threadIdx.x == 0) {
+    const uint32_t s0 = c.sid ? c.sid[k0] : 0u;
+    const uint32_t s1 = c.sid ? c.sid[k1] : 0u;
+    const SceneDesc &sc = c.scenes[s0];
+    const uint32_t nx = (uint32_t)sc.ncell[0];
+    const uint32_t a = c.skeys[k0] - sc.cell_base, b = c.skeys[k1] - sc.cell_base;
+    const uint32_t ra = a / nx, rb = b / nx;
+    w.scene = s0;
+    w.row_a = ra;
+    w.nparts = (s0 == s1 && rb >= ra && rb <= ra + 1u) ? (rb - ra + 1u) : 0u;
+    w.xa[0] = a % nx;
+    w.xb[0] = rb == ra ? b % nx : nx - 1u;
+    w.xa[1] = 0;
+    w.xb[1] = b % nx;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const uint32_t t = threadIdx.x, part = t / 9u, q = t % 9u;
+    uint32_t S = 0, L = 0;
+    if (t < 18 && part < w.nparts) {
+      const SceneDesc &sc = c.scenes[w.scene];
+      const uint32_t nx = (uint32_t)sc.ncell[0], ny = (uint32_t)sc.ncell[1], nz = (uint32_t)sc.ncell[2];
+      const uint32_t row = w.row_a + part;
+      const int yy = (int)(row % ny) + (int)(q % 3u) - 1;
+      const int zz = (int)(row / ny) + (int)(q / 3u) - 1;
+      if (yy >= 0 && yy < (int)ny && zz >= 0 && zz < (int)nz) {
+        const uint32_t rk = sc.cell_base + nx * ((uint32_t)yy + ny * (uint32_t)zz);
+        const uint32_t lo = rk + (w.xa[part] > 0 ? w.xa[part] - 1u : 0u);
+        const uint32_t hi = rk + min(w.xb[part] + 1u, nx - 1u);
+        S = __ldg(&c.off[lo]);
+        L = __ldg(&c.off[hi + 1]) - S;
+      }
+    }
+    w.S[t] = S;
+    w.len[t] = L;
+    // Lists can encode the tile iff it has a row decomposition and every
+    // range fits the 11-bit offset (always, short of a hundred particles per
+    // cell); otherwise the whole tile takes the fallback.
+    const bool fits = __all_sync(0xffffffffu, L <= kRelMax && (uint64_t)S + L <= c.n);
+    if (t == 0) w.listed = (w.nparts > 0 && fits) ? 1u : 0u;
+  }
+  __syncthreads();
+  return true;
+}
+
+// Slot of list entry e: S[range] + offset, clamped so that a stale entry
+// can never address past the arrays.
+__device__ __forceinline__ uint32_t entry_slot(const Ranges &w, uint32_t e, uint32_t n) {
+  return min(w.S[(e >> kRelBits) & 31u] + (e & (kRelMax - 1u)), n - 1u);
+}
+
+// For the `cnt` listed neighbours of particle k: per group of eight, first
+// load(slot) for all eight (unconditionally; past-the-end entries read a
+// valid slot), then f(data, valid) for each -- so that the eight gathers are
+// in flight together instead of one after another.
+template <typename Load, typename F>
+__device__ __forceinline__ void for_each_listed(const NbrCtx &c, const Ranges &w, uint32_t k,
+                                                uint32_t cnt, Load &&load, F &&f) {
+  const uint32_t groups = (cnt + 7u) >> 3;
+  for (uint32_t g = 0; g < groups; ++g) {
+    const uint4 v = __ldg(&c.nbr4[(size_t)g * c.n + k]);
+    const uint32_t rem = cnt - (g << 3);
+    const uint32_t words[4] = {v.x, v.y, v.z, v.w};
+    decltype(load(0u)) data[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+      data[e] = load(entry_slot(w, (words[e >> 1] >> ((e & 1) * 16)) & 0xFFFFu, c.n));
+#pragma unroll
+    for (int e = 0; e < 8; ++e) f(data[e], (uint32_t)e < rem);
+  }
+}
+
+// Accumulates one particle's list entries and writes them a group at a time.
+struct ListWriter {
+  uint64_t lo = 0, hi = 0;
+  __device__ __forceinline__ void put(uint4 *nbr4, uint32_t n, uint32_t k, uint32_t slot,
+                                      uint32_t e16) {
+    const uint32_t e = slot & 7u;
+    if (e < 4) lo |= (uint64_t)e16 << (16u * e);
+    else hi |= (uint64_t)e16 << (16u * (e - 4u));
+    if (e == 7u) flush(nbr4, n, k, slot >> 3);
+  }
+  __device__ __forceinline__ void flush(uint4 *nbr4, uint32_t n, uint32_t k, uint32_t group) {
+    nbr4[(size_t)group * n + k] =
+        make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
+    lo = hi = 0;
+  }
+};
+
 // v' = v + dt g;  d = dt v';  p = x + d  -- rounded op by op (no
 // contraction) so that every kernel that recomputes them gets the same bits.
-__device__ __forceinline__ float4 gravity_velocity(float4 v, float dt,
-                                                   float gy) {
+__device__ __forceinline__ float4 gravity_velocity(float4 v, float dt, float gy) {
   v.y = __fadd_rn(v.y, __fmul_rn(dt, gy));
   return v;
 }
 __device__ __forceinline__ float3 displacement(float4 v1, float dt) {
-  return make_float3(__fmul_rn(dt, v1.x), __fmul_rn(dt, v1.y),
-                     __fmul_rn(dt, v1.z));
+  return make_float3(__fmul_rn(dt, v1.x), __fmul_rn(dt, v1.y), __fmul_rn(dt, v1.z));
 }
 __device__ __forceinline__ float3 add3(float4 x, float3 d) {
-  return make_float3(__fadd_rn(x.x, d.x), __fadd_rn(x.y, d.y),
-                     __fadd_rn(x.z, d.z));
+  return make_float3(__fadd_rn(x.x, d.x), __fadd_rn(x.y, d.y), __fadd_rn(x.z, d.z));
 }
 
 // Step-start predicted position of slot j (as written by the reorder).
@@ -73,13 +205,11 @@ __device__ __forceinline__ float3 start_position(const NbrCtx &c, uint32_t j) {
   return add3(__ldg(&c.X2[j]), displacement(__ldg(&c.V2[j]), c.dt));
 }
 
-// Visits the particles of the 27 cells around the cell with key `key`, in
-// the order (dz, dy, sorted slot), skipping k itself.
+// Visits the 9 rows around the cell with key `key` (order: dz, dy, slot);
+// f(q, j) gets the row index q = (dz+1)*3 + (dy+1) and the slot j != k.
 template <typename F>
-__device__ __forceinline__ void scan_cells(uint32_t k, uint32_t key,
-                                           const SceneDesc &s,
-                                           const uint32_t *__restrict__ off,
-                                           F &&f) {
+__device__ __forceinline__ void scan_rows(uint32_t k, uint32_t key, const SceneDesc &s,
+                                          const uint32_t *__restrict__ off, F &&f) {
   const int nx = s.ncell[0], ny = s.ncell[1], nz = s.ncell[2];
   const uint32_t local = key - s.cell_base;
   const int cx = (int)(local % (uint32_t)nx);
@@ -94,33 +224,76 @@ __device__ __forceinline__ void scan_cells(uint32_t k, uint32_t key,
     for (int dy = -1; dy <= 1; ++dy) {
       const int y = cy + dy;
       if (y < 0 || y >= ny) continue;
-      const uint32_t row =
-          s.cell_base + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+      const int q = (dz + 1) * 3 + (dy + 1);
+      const uint32_t row = s.cell_base + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
       const uint32_t a = __ldg(&off[row + x0]);
       const uint32_t b = __ldg(&off[row + x1 + 1]);
       for (uint32_t j = a; j < b; ++j)
-        if (j != k) f(j);
+        if (j != k) f(q, j);
     }
   }
 }
 
-// Visits N_k: from the list, or (list overflow) from the cells with the
-// membership test at the step-start positions, in the same order.
-template <typename F>
-__device__ __forceinline__ void visit_neighbours(const NbrCtx &c, uint32_t k,
-                                                 uint32_t count, F &&f) {
-  if (count <= c.maxn) {
-    for (uint32_t s = 0; s < count; ++s) f(__ldg(&c.nbr[(size_t)s * c.n + k]));
-  } else {
-    const SceneDesc &sc = scene_of(c.scenes, c.sid, k);
-    const float3 pk = start_position(c, k);
-    scan_cells(k, __ldg(&c.skeys[k]), sc, c.off, [&](uint32_t j) {
-      const float3 pj = start_position(c, j);
-      const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
-      const float r2 = rx * rx + ry * ry + rz * rz;
-      if (r2 > 0.0f && r2 < c.h2) f(j);
-    });
+// scan_rows with the candidates of a row taken four at a time: the four
+// loads are issued before any is used.  f(q, j, data, valid).
+template <typename Load, typename F>
+__device__ __forceinline__ void scan_rows_batched(uint32_t k, uint32_t key, const SceneDesc &s,
+                                                  const uint32_t *__restrict__ off, Load &&load,
+                                                  F &&f) {
+  const int nx = s.ncell[0], ny = s.ncell[1], nz = s.ncell[2];
+  const uint32_t local = key - s.cell_base;
+  const int cx = (int)(local % (uint32_t)nx);
+  const uint32_t t = local / (uint32_t)nx;
+  const int cy = (int)(t % (uint32_t)ny);
+  const int cz = (int)(t / (uint32_t)ny);
+  const int x0 = cx > 0 ? cx - 1 : 0;
+  const int x1 = cx + 1 < nx ? cx + 1 : nx - 1;
+  for (int dz = -1; dz <= 1; ++dz) {
+    const int z = cz + dz;
+    if (z < 0 || z >= nz) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = cy + dy;
+      if (y < 0 || y >= ny) continue;
+      const int q = (dz + 1) * 3 + (dy + 1);
+      const uint32_t row = s.cell_base + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+      const uint32_t a = __ldg(&off[row + x0]);
+      const uint32_t b = __ldg(&off[row + x1 + 1]);
+      for (uint32_t j = a; j < b; j += 4) {
+        decltype(load(0u)) data[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) data[e] = load(min(j + e, b - 1u));
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const uint32_t je = j + e;
+          f(q, je, data[e], je < b && je != k);
+        }
+      }
+    }
   }
+}
+
+// Re-derives N_k from the cells and the step-start positions (global loads).
+template <typename F>
+__device__ __forceinline__ void visit_fallback(const NbrCtx &c, uint32_t k, F &&f) {
+  const SceneDesc &sc = scene_of(c.scenes, c.sid, k);
+  const float3 pk = start_position(c, k);
+  scan_rows(k, __ldg(&c.skeys[k]), sc, c.off, [&](int, uint32_t j) {
+    const float3 pj = start_position(c, j);
+    const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
+    const float r2 = rx * rx + ry * ry + rz * rz;
+    if (r2 > 0.0f && r2 < c.h2) f(j);
+  });
+}
+
+// Calls f(load(slot), true) for every neighbour of particle k (and, in the
+// listed path, f(..., false) for the padding of the last group): from the
+// list when the tile is listed and k's set fits, otherwise re-derived.
+template <typename Load, typename F>
+__device__ __forceinline__ void visit_neighbours(const NbrCtx &c, const Ranges &w, uint32_t k,
+                                                 Load &&load, F &&f) {
+  const uint32_t cnt = c.cnt[k];
+  if (w.listed && cnt <= c.maxn) for_each_listed(c, w, k, cnt, load, f);
+  else visit_fallback(c, k, [&](uint32_t j) { f(load(j), true); });
 }
 
 __device__ __forceinline__ float ipow(float b, int e) {
@@ -131,6 +304,17 @@ __device__ __forceinline__ float ipow(float b, int e) {
     e >>= 1;
   }
   return r;
+}
+
+// -k h^2 (W(r)/W(dq h))^n with W(r)/W(dq h) = ((h^2-r^2)/(h^2-dq^2 h^2))^3.
+__device__ __forceinline__ float scorr_term(float r2, const PaperConsts &c) {
+  const float ratio = (c.h2 - r2) * c.inv_scorr_den;
+  if (c.scorr_n3 == 12) {
+    const float r3 = ratio * ratio * ratio;
+    const float r6 = r3 * r3;
+    return -c.scorr_k * (r6 * r6);
+  }
+  return -c.scorr_k * ipow(ratio, c.scorr_n3);
 }
 
 // Spiky gradient factor: grad_i W(r_vec) = f * r_vec, f = -S (h-r)^2 / r.
@@ -207,70 +391,84 @@ __global__ void __launch_bounds__(256)
   D[k] = make_float4(d.x, d.y, d.z, 0.0f);
 }
 
-__global__ void __launch_bounds__(kGatherThreads)
+// Neighbour-list build over the 27 cells, fused with the first lambda pass.
+__global__ void __launch_bounds__(kTile)
     k_nbr_lambda(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
-                 uint32_t *__restrict__ nbr, uint32_t *__restrict__ nbr_cnt,
+                 uint4 *__restrict__ nbr4, uint32_t *__restrict__ nbr_cnt,
                  float4 *__restrict__ Q, float *__restrict__ R) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ Ranges w;
+  if (!ranges_setup(w, blockIdx.x, nc)) return;
+  const uint32_t k = blockIdx.x * kTile + threadIdx.x;
   if (k >= c.n) return;
+  const bool listed = w.listed != 0;
+  const SceneDesc &sc = nc.scenes[w.scene];
   const float4 pk = P[k];
-  const SceneDesc &sc = scene_of(nc.scenes, nc.sid, k);
   LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
+  ListWriter lw;
   uint32_t cnt = 0;
-  scan_cells(k, nc.skeys[k], sc, nc.off, [&](uint32_t j) {
-    const float4 pj = __ldg(&P[j]);
+  const uint32_t key = nc.skeys[k];
+  // Which of the tile's rows (parts) this particle belongs to.
+  const uint32_t part = (key - sc.cell_base) / (uint32_t)sc.ncell[0] == w.row_a ? 0u : 9u;
+  scan_rows_batched(k, key, sc, nc.off, [&](uint32_t j) { return __ldg(&P[j]); },
+                    [&](int q0, uint32_t j, float4 pj, bool valid) {
     const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
-    if (r2 > 0.0f && r2 < c.h2) {
-      if (cnt < c.maxn) nbr[(size_t)cnt * c.n + k] = j;
+    if (valid && r2 > 0.0f && r2 < c.h2) {
+      const uint32_t q = part + (uint32_t)q0;
+      const uint32_t rel = j - w.S[q];
+      if (listed && cnt < c.maxn) lw.put(nbr4, c.n, k, cnt, (q << kRelBits) | (rel & (kRelMax - 1u)));
       ++cnt;
       acc.add(rx, ry, rz, r2, c);
     }
   });
+  if (listed && cnt <= c.maxn && (cnt & 7u)) lw.flush(nbr4, c.n, k, cnt >> 3);
   nbr_cnt[k] = cnt;
   Q[k] = make_float4(pk.x, pk.y, pk.z, acc.lambda(c));
   R[k] = acc.rho;
 }
 
-__global__ void __launch_bounds__(kGatherThreads)
+__global__ void __launch_bounds__(kTile)
     k_lambda(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
              float4 *__restrict__ Q, float *__restrict__ R) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ Ranges w;
+  if (!ranges_setup(w, blockIdx.x, nc)) return;
+  const uint32_t k = blockIdx.x * kTile + threadIdx.x;
   if (k >= c.n) return;
   const float4 pk = P[k];
   LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
-  visit_neighbours(nc, k, nc.cnt[k], [&](uint32_t j) {
-    const float4 pj = __ldg(&P[j]);
-    const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
-    const float r2 = rx * rx + ry * ry + rz * rz;
-    if (r2 > 0.0f && r2 < c.h2) acc.add(rx, ry, rz, r2, c);
-  });
+  visit_neighbours(
+      nc, w, k, [&](uint32_t j) { return __ldg(&P[j]); },
+      [&](float4 pj, bool valid) {
+        const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
+        const float r2 = rx * rx + ry * ry + rz * rz;
+        if (valid && r2 > 0.0f && r2 < c.h2) acc.add(rx, ry, rz, r2, c);
+      });
   Q[k] = make_float4(pk.x, pk.y, pk.z, acc.lambda(c));
   R[k] = acc.rho;
 }
 
-__global__ void __launch_bounds__(kGatherThreads)
+__global__ void __launch_bounds__(kTile)
     k_delta(const float4 *__restrict__ Q, NbrCtx nc, PaperConsts c,
             float4 *__restrict__ D, float4 *__restrict__ P,
             const float *__restrict__ R, float4 *__restrict__ U, int last) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ Ranges w;
+  if (!ranges_setup(w, blockIdx.x, nc)) return;
+  const uint32_t k = blockIdx.x * kTile + threadIdx.x;
   if (k >= c.n) return;
   const float4 qk = Q[k];
   float sx = 0.f, sy = 0.f, sz = 0.f;
-  visit_neighbours(nc, k, nc.cnt[k], [&](uint32_t j) {
-    const float4 qj = __ldg(&Q[j]);
-    const float rx = qk.x - qj.x, ry = qk.y - qj.y, rz = qk.z - qj.z;
-    const float r2 = rx * rx + ry * ry + rz * rz;
-    if (r2 > 0.0f && r2 < c.h2) {
-      const float f = spiky_factor(r2, c);
-      const float ratio = (c.h2 - r2) * c.inv_scorr_den;
-      const float scorr = -c.scorr_k * ipow(ratio, c.scorr_n3);
-      const float w = (qk.w + qj.w + scorr) * f;
-      sx += w * rx;
-      sy += w * ry;
-      sz += w * rz;
-    }
-  });
+  visit_neighbours(
+      nc, w, k, [&](uint32_t j) { return __ldg(&Q[j]); },
+      [&](float4 qj, bool valid) {
+        const float rx = qk.x - qj.x, ry = qk.y - qj.y, rz = qk.z - qj.z;
+        const float r2 = rx * rx + ry * ry + rz * rz;
+        if (valid && r2 > 0.0f && r2 < c.h2) {
+          const float wgt = (qk.w + qj.w + scorr_term(r2, c)) * spiky_factor(r2, c);
+          sx += wgt * rx;
+          sy += wgt * ry;
+          sz += wgt * rz;
+        }
+      });
   const float4 x = nc.X2[k];
   const float4 d0 = D[k];
   float3 d = make_float3(d0.x + sx * c.inv_rho0, d0.y + sy * c.inv_rho0,
@@ -292,20 +490,29 @@ __global__ void __launch_bounds__(kGatherThreads)
                        __fdiv_rn(d.z, c.dt), 1.0f / R[k]);
 }
 
-__global__ void __launch_bounds__(kGatherThreads)
+// Vorticity omega_k; also writes (p_k, |omega_k|) into PW for the next pass.
+__global__ void __launch_bounds__(kTile)
     k_vorticity(const float4 *__restrict__ P, const float4 *__restrict__ U,
-                NbrCtx nc, PaperConsts c, float4 *__restrict__ Wo) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+                NbrCtx nc, PaperConsts c, float4 *__restrict__ Wo,
+                float4 *__restrict__ PW) {
+  __shared__ Ranges w;
+  if (!ranges_setup(w, blockIdx.x, nc)) return;
+  const uint32_t k = blockIdx.x * kTile + threadIdx.x;
   if (k >= c.n) return;
   const float4 pk = P[k];
   const float4 uk = U[k];
   float wx = 0.f, wy = 0.f, wz = 0.f;
-  visit_neighbours(nc, k, nc.cnt[k], [&](uint32_t j) {
-    const float4 pj = __ldg(&P[j]);
+  struct PU {
+    float4 p, u;
+  };
+  visit_neighbours(
+      nc, w, k, [&](uint32_t j) { return PU{__ldg(&P[j]), __ldg(&U[j])}; },
+      [&](const PU &d, bool valid) {
+    const float4 pj = d.p;
     const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
-    if (r2 > 0.0f && r2 < c.h2) {
-      const float4 uj = __ldg(&U[j]);
+    if (valid && r2 > 0.0f && r2 < c.h2) {
+      const float4 uj = d.u;
       const float f = spiky_factor(r2, c) * uj.w;
       const float gx = f * rx, gy = f * ry, gz = f * rz;
       const float ux = uj.x - uk.x, uy = uj.y - uk.y, uz = uj.z - uk.z;
@@ -314,28 +521,36 @@ __global__ void __launch_bounds__(kGatherThreads)
       wz += gx * uy - gy * ux;
     }
   });
-  Wo[k] = make_float4(wx, wy, wz, sqrtf(wx * wx + wy * wy + wz * wz));
+  const float wn = sqrtf(wx * wx + wy * wy + wz * wz);
+  Wo[k] = make_float4(wx, wy, wz, wn);
+  PW[k] = make_float4(pk.x, pk.y, pk.z, wn);
 }
 
-__global__ void __launch_bounds__(kGatherThreads)
-    k_xsph_commit(const float4 *__restrict__ P, const float4 *__restrict__ U,
+__global__ void __launch_bounds__(kTile)
+    k_xsph_commit(const float4 *__restrict__ PW, const float4 *__restrict__ U,
                   const float4 *__restrict__ Wv, NbrCtx nc, PaperConsts c,
                   const uint32_t *__restrict__ ID2, float4 *__restrict__ X,
                   float4 *__restrict__ V, uint32_t *__restrict__ ID) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ Ranges w;
+  if (!ranges_setup(w, blockIdx.x, nc)) return;
+  const uint32_t k = blockIdx.x * kTile + threadIdx.x;
   if (k >= c.n) return;
-  const float4 pk = P[k];
+  const float4 pk = PW[k];
   const float4 uk = U[k];
   const float4 wk = Wv[k];
   float ex = 0.f, ey = 0.f, ez = 0.f, xx = 0.f, xy = 0.f, xz = 0.f;
-  visit_neighbours(nc, k, nc.cnt[k], [&](uint32_t j) {
-    const float4 pj = __ldg(&P[j]);
+  struct PU {
+    float4 p, u;
+  };
+  visit_neighbours(
+      nc, w, k, [&](uint32_t j) { return PU{__ldg(&PW[j]), __ldg(&U[j])}; },
+      [&](const PU &d, bool valid) {
+    const float4 pj = d.p;
     const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
-    if (r2 > 0.0f && r2 < c.h2) {
-      const float4 uj = __ldg(&U[j]);
-      const float wn = __ldg(&Wv[j].w);
-      const float e = spiky_factor(r2, c) * uj.w * (wn - wk.w);
+    if (valid && r2 > 0.0f && r2 < c.h2) {
+      const float4 uj = d.u;
+      const float e = spiky_factor(r2, c) * uj.w * (pj.w - wk.w);
       ex += e * rx;
       ey += e * ry;
       ez += e * rz;
@@ -405,10 +620,9 @@ inline uint32_t blocks_for(uint64_t n, uint32_t t) {
   return (uint32_t)((n + t - 1) / t);
 }
 
-NbrCtx make_ctx(const DeviceState &d, const PaperConsts &c,
-                const uint16_t *sid) {
+NbrCtx make_ctx(const DeviceState &d, const PaperConsts &c, const uint16_t *sid) {
   NbrCtx nc;
-  nc.nbr = d.nbr;
+  nc.nbr4 = d.nbr;
   nc.cnt = d.nbr_cnt;
   nc.skeys = d.skeys;
   nc.off = d.offsets;
@@ -416,6 +630,7 @@ NbrCtx make_ctx(const DeviceState &d, const PaperConsts &c,
   nc.V2 = d.V2;
   nc.scenes = d.scenes;
   nc.sid = sid;
+  nc.err = d.err;
   nc.n = c.n;
   nc.maxn = c.maxn;
   nc.dt = c.dt;
@@ -424,6 +639,10 @@ NbrCtx make_ctx(const DeviceState &d, const PaperConsts &c,
 }
 
 }  // namespace
+
+uint32_t paper_tiles(uint32_t n) { return gather_tiles(n); }
+
+cudaError_t paper_configure() { return cudaSuccess; }
 
 cudaError_t paper_predict_hash(const float4 *X, const float4 *V, uint32_t n,
                                const PaperConsts &c, const SceneDesc *scenes,
@@ -440,43 +659,40 @@ cudaError_t paper_reorder(const uint32_t *perm, const float4 *X,
                           const PaperConsts &c, float4 *X2, float4 *V2,
                           uint32_t *ID2, float4 *P, float4 *D,
                           cudaStream_t st) {
-  k_reorder<<<blocks_for(n, 256), 256, 0, st>>>(perm, X, V, ID, n, c, X2, V2,
-                                                 ID2, P, D);
+  k_reorder<<<blocks_for(n, 256), 256, 0, st>>>(perm, X, V, ID, n, c, X2, V2, ID2, P, D);
   return cudaGetLastError();
 }
 
 cudaError_t paper_nbr_lambda(const DeviceState &d, const PaperConsts &c,
                              const uint16_t *sid, cudaStream_t st) {
-  k_nbr_lambda<<<blocks_for(c.n, kGatherThreads), kGatherThreads, 0, st>>>(
-      d.P, make_ctx(d, c, sid), c, d.nbr, d.nbr_cnt, d.Q, d.R);
+  k_nbr_lambda<<<c.tiles, kTile, 0, st>>>(d.P, make_ctx(d, c, sid), c, d.nbr, d.nbr_cnt,
+                                          d.Q, d.R);
   return cudaGetLastError();
 }
 
 cudaError_t paper_lambda(const DeviceState &d, const PaperConsts &c,
                          const uint16_t *sid, cudaStream_t st) {
-  k_lambda<<<blocks_for(c.n, kGatherThreads), kGatherThreads, 0, st>>>(
-      d.P, make_ctx(d, c, sid), c, d.Q, d.R);
+  k_lambda<<<c.tiles, kTile, 0, st>>>(d.P, make_ctx(d, c, sid), c, d.Q, d.R);
   return cudaGetLastError();
 }
 
 cudaError_t paper_delta(const DeviceState &d, const PaperConsts &c,
                         const uint16_t *sid, bool last, cudaStream_t st) {
-  k_delta<<<blocks_for(c.n, kGatherThreads), kGatherThreads, 0, st>>>(
-      d.Q, make_ctx(d, c, sid), c, d.D, d.P, d.R, d.U, last ? 1 : 0);
+  k_delta<<<c.tiles, kTile, 0, st>>>(d.Q, make_ctx(d, c, sid), c, d.D, d.P, d.R, d.U,
+                                     last ? 1 : 0);
   return cudaGetLastError();
 }
 
 cudaError_t paper_vorticity(const DeviceState &d, const PaperConsts &c,
                             const uint16_t *sid, cudaStream_t st) {
-  k_vorticity<<<blocks_for(c.n, kGatherThreads), kGatherThreads, 0, st>>>(
-      d.P, d.U, make_ctx(d, c, sid), c, d.W);
+  k_vorticity<<<c.tiles, kTile, 0, st>>>(d.P, d.U, make_ctx(d, c, sid), c, d.W, d.D);
   return cudaGetLastError();
 }
 
 cudaError_t paper_xsph_commit(const DeviceState &d, const PaperConsts &c,
                               const uint16_t *sid, cudaStream_t st) {
-  k_xsph_commit<<<blocks_for(c.n, kGatherThreads), kGatherThreads, 0, st>>>(
-      d.P, d.U, d.W, make_ctx(d, c, sid), c, d.ID2, d.X, d.V, d.ID);
+  k_xsph_commit<<<c.tiles, kTile, 0, st>>>(d.D, d.U, d.W, make_ctx(d, c, sid), c, d.ID2,
+                                           d.X, d.V, d.ID);
   return cudaGetLastError();
 }
 

@@ -88,7 +88,9 @@ PaperConsts make_paper_consts(const pbf_params &p, uint32_t n) {
   c.xsph_c = p.xsph_c;
   c.vort_eps = p.vort_eps;
   c.n = n;
-  c.maxn = p.max_neighbours;
+  // Lists are stored in groups of eight entries.
+  c.maxn = p.max_neighbours < 8 ? 8u : (p.max_neighbours / 8u) * 8u;
+  c.tiles = 0;
   return c;
 }
 

@@ -277,6 +277,7 @@ int pbf_create(const pbf_params *params, const pbf_particle *particles,
   s->rc = make_ref_consts(*params);
   s->rc.n = n;
   s->pc = make_paper_consts(*params, n);
+  s->pc.tiles = paper_tiles(n);
   s->plan = make_sort_plan(n, bits_for(s->ncells));
   *out = s.release();
   return PBF_OK;
@@ -286,6 +287,7 @@ int pbf_init(pbf_sim *s) {
   if (!s) return PBF_ERR_INVALID;
   if (s->inited) return PBF_ERR_STATE;
   PBF_TRY(cudaGetDevice(&s->device));
+  if (s->paper) PBF_TRY(paper_configure());
   PBF_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
   DeviceState &d = s->d;
   const size_t n = s->n;
@@ -316,7 +318,7 @@ int pbf_init(pbf_sim *s) {
     A(&d.W, n);
     A(&d.R, n);
     A(&d.nbr_cnt, n);
-    A(&d.nbr, (size_t)s->prm.max_neighbours * n);
+    A(&d.nbr, (size_t)(s->pc.maxn / 8u) * n);
   } else {
     A(&d.P2, n);
     A(&d.DV, n);
