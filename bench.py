@@ -345,19 +345,154 @@ def run_ours(args) -> int:
     return 0
 
 
+def plain_one_by_one(pbf, scenes, steps: int, sample_steps: int, ext_stream_of):
+    """The scenes solved one at a time on the plain path: per scene, create,
+    upload, warm up, then time `sample_steps` graph-replayed steps with CUDA
+    events.  Returns per-scene seconds for `steps` steps (sampled rate x
+    steps) and the wall seconds of set-up plus read-back per scene."""
+    import torch
+
+    step_s, setup_s = [], []
+    for s in scenes:
+        w0 = time.perf_counter()
+        sim = pbf.Simulation(s.params, s.particles)
+        sim.init()
+        sim.step(3)
+        ext = ext_stream_of(sim)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        sim.step(sample_steps, sync=False)
+        e1.record(ext)
+        e1.synchronize()
+        sim.sync()
+        t = e0.elapsed_time(e1) / 1e3 / sample_steps * steps
+        sim.dumpData()
+        sim.close()
+        step_s.append(t)
+        setup_s.append(time.perf_counter() - w0 - e0.elapsed_time(e1) / 1e3)
+    return step_s, setup_s
+
+
+def run_batch(args) -> int:
+    """256 independent dam-break scenes of log-uniform sizes advanced together
+    (one launch per kernel per step, CUDA-graph step) against the same scenes
+    solved one at a time on the plain path."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    world, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    dist = make_group(world, "nccl")
+    pbf = ge.load_package()
+    scenes = pbf.scenes.mixed_batch(256)
+    steps = args.steps
+    n_tot = sum(s.n for s in scenes)
+    cells_tot = sum(s.params.ncells for s in scenes)
+    solver = scenes[0].params
+
+    # ---- end to end: upload every scene, step, read every scene back ------
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    b = pbf.Batch(solver, len(scenes), n_tot, cells_tot)
+    ids = [b.add_scene(s.params, s.particles) for s in scenes]
+    ext = torch.cuda.ExternalStream(b.stream())
+    launches = b.launches_per_step()
+    b.step(args.warmup)
+    b.sync()
+    # ---- device-resident throughput ------------------------------------
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        e0.record(ext)
+        b.step(steps, sync=False)
+        e1.record(ext)
+        e1.synchronize()
+    b.sync()
+    finite = all(bool(np.isfinite(b.dump_scene(i)[0]).all()) for i in ids)
+    t_wall = time.perf_counter() - w0
+    b.close()
+    t_dev = reduce_max(dist, e0.elapsed_time(e1) / 1e3, device="cuda")
+    value = world * n_tot * ITERATIONS * steps / t_dev
+    work_e2e = n_tot * ITERATIONS * (steps + args.warmup)
+    t_wall = reduce_max(dist, t_wall, device="cuda")
+    e2e_value = world * work_e2e / t_wall
+    peaks = measured_peaks()
+    sort_bits = int(np.ceil(np.log2(max(cells_tot, 2))))
+    step_bytes = STEP_BYTES - 52 + 4 + 16 * ((sort_bits + 7) // 8)
+    step_gbs = step_bytes * n_tot / (t_dev / steps) / 1e9
+
+    # ---- the same scenes one by one on the plain path ---------------------
+    plain = None
+    if rank == 0 and not args.no_plain:
+        sample = max(3, min(steps, args.plain_sample))
+        plain_step_s, plain_setup_s = plain_one_by_one(
+            pbf, scenes, steps, sample, lambda sim: torch.cuda.ExternalStream(sim.stream()))
+        t_plain = sum(plain_step_s)
+        done = np.cumsum([a + c for a, c in zip(plain_step_s, plain_setup_s)])
+        plain = {"value": n_tot * ITERATIONS * steps / t_plain, "unit": UNIT,
+                 "seconds_device": t_plain,
+                 "scene_latency_s": {"p50": float(np.percentile(done, 50)),
+                                     "p99": float(np.percentile(done, 99))},
+                 "method": f"each scene alone through the plain C-ABI path (CUDA-graph steps); "
+                           f"{sample} timed steps per scene after 3 warm-up steps, scaled to {steps}; "
+                           f"latency = completion time of scene k when solved in sequence"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": t_dev / steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch_256_scenes", "scenes": len(scenes), "particles": n_tot,
+                       "cells": cells_tot, "sizes": "log-uniform 4096..262144, seed 0x5EED",
+                       "solver_iterations": ITERATIONS, "graph": True,
+                       "equations": "paper (relaxation 600, s_corr, XSPH, vorticity)",
+                       "l2": "working set larger than L2; no flush between steps"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n_tot / (steps + args.warmup),
+                    "d2h_bytes_per_step": 32 * n_tot / (steps + args.warmup),
+                    "method": "wall clock from batch creation through upload of every scene, "
+                              f"{args.warmup}+{steps} steps and read-back of every scene",
+                    "finite": finite},
+            "gpu_launches": launches * steps,
+            "step_roofline": {"bytes_per_particle_step": step_bytes, "achieved_gbs": step_gbs,
+                              "frac": step_gbs / peaks["hbm_gbs"], "peak_source": peaks["source"]},
+            "scene_latency_s": {"p50": t_wall, "p99": t_wall,
+                                "note": "every scene of the batch completes with the last step"},
+            "plain_one_by_one": plain,
+            "speedup_vs_plain": (value / plain["value"]) if plain else None,
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 500 for the single scene, 300 for the batch)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["single", "batch"], default="single")
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--plain-sample", type=int, default=30,
+                    help="timed steps per scene of the one-by-one plain comparison")
+    ap.add_argument("--no-plain", action="store_true", help="skip the one-by-one plain comparison")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.steps is None:
+        args.steps = 300 if args.workload == "batch" else 500
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
     return run_ours(args)
 
 

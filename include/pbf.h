@@ -216,6 +216,44 @@ int pbf_get_cells(pbf_sim *sim, uint32_t *hash, uint32_t *perm,
                   int32_t *ranges);
 int pbf_destroy(pbf_sim *sim);
 
+/* ------------------------------------------------------ batched scenes */
+/* Many independent scenes advanced together (no counterpart in the
+ * reference, which runs one scene): one sort over scene-major keys (scene s
+ * owns the key range [cell_base_s, cell_base_s + cells_s), i.e. the scene in
+ * the high-order part of the key), one launch per kernel for all scenes, and
+ * each step replayed as one CUDA graph.  A scene's trajectory is the same,
+ * bit for bit, alone (pbf_sim) and in any mix.
+ *
+ * Solver settings come from `solver` (mode must be PBF_MODE_PAPER; time
+ * step, rest density, h = (x_max - x_min) / x_n, iterations, relaxation,
+ * s_corr, XSPH, vorticity, gravity, max_neighbours).  Each scene brings its
+ * own box, grid and wall margin.  Capacities fix the device allocation. */
+typedef struct pbf_batch pbf_batch;
+int pbf_batch_create(const pbf_params *solver, uint32_t max_scenes,
+                     uint32_t max_particles, uint32_t max_cells,
+                     pbf_batch **out);
+/* Device bytes a batch with these capacities allocates. */
+size_t pbf_batch_device_bytes(const pbf_params *solver, uint32_t max_scenes,
+                              uint32_t max_particles, uint32_t max_cells);
+/* Adds a scene; *scene_id identifies it until removal.  Takes effect at the
+ * next step.  PBF_ERR_BUDGET if a capacity would be exceeded. */
+int pbf_batch_add_scene(pbf_batch *b, const pbf_params *scene,
+                        const pbf_particle *particles, uint32_t n,
+                        uint32_t *scene_id);
+int pbf_batch_remove_scene(pbf_batch *b, uint32_t scene_id);
+/* Advances every scene `nsteps` steps, enqueued on the batch's stream. */
+int pbf_batch_step(pbf_batch *b, uint32_t nsteps);
+int pbf_batch_sync(pbf_batch *b);
+/* State of one scene in its input particle order (dumpData layout). */
+int pbf_batch_dump_scene(pbf_batch *b, uint32_t scene_id, float *pos4,
+                         float *vel4);
+int pbf_batch_set_wave(pbf_batch *b, uint32_t scene_id, float value);
+int pbf_batch_info(const pbf_batch *b, uint32_t *scenes, uint32_t *particles,
+                   uint32_t *cells);
+int pbf_batch_get_stream(const pbf_batch *b, void **stream);
+int pbf_batch_launches_per_step(const pbf_batch *b, uint32_t *launches);
+int pbf_batch_destroy(pbf_batch *b);
+
 /* ------------------------------------ neighbour-structure operators (L4) */
 /* Cell hash of N predicted positions (float4, .w ignored) on the grid of
  * `params` (update_cells.cl:10-15 / calc_hash.cl:15-20).  Each axis cell

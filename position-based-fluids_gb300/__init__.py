@@ -155,6 +155,18 @@ def lib():
             "pbf_op_sort_pairs_noalloc": ([vp, vp, u32, u32, vp, vp, vp, vp], i32),
             "pbf_op_cell_offsets": ([vp, u32, u32, vp, vp], i32),
             "pbf_op_find_cells": ([vp, u32, vp, vp], i32),
+            "pbf_batch_create": ([pp, u32, u32, u32, C.POINTER(vp)], i32),
+            "pbf_batch_device_bytes": ([pp, u32, u32, u32], C.c_size_t),
+            "pbf_batch_add_scene": ([vp, pp, vp, u32, C.POINTER(u32)], i32),
+            "pbf_batch_remove_scene": ([vp, u32], i32),
+            "pbf_batch_step": ([vp, u32], i32),
+            "pbf_batch_sync": ([vp], i32),
+            "pbf_batch_dump_scene": ([vp, u32, vp, vp], i32),
+            "pbf_batch_set_wave": ([vp, u32, f32], i32),
+            "pbf_batch_info": ([vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)], i32),
+            "pbf_batch_get_stream": ([vp, C.POINTER(vp)], i32),
+            "pbf_batch_launches_per_step": ([vp, C.POINTER(u32)], i32),
+            "pbf_batch_destroy": ([vp], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -373,6 +385,90 @@ class Simulation:
         n = C.c_uint32()
         _check(lib().pbf_launches_per_step(self._h, C.byref(n)), "pbf_launches_per_step")
         return n.value
+
+
+class Batch:
+    """Many paper-mode scenes advanced together (pbf_batch_* in include/pbf.h).
+
+    `solver` carries the shared solver settings (h, iterations, s_corr,
+    XSPH, vorticity); each scene brings its own box, grid and walls."""
+
+    def __init__(self, solver: Params, max_scenes: int, max_particles: int, max_cells: int):
+        self.solver = solver.copy()
+        h = C.c_void_p()
+        _check(lib().pbf_batch_create(C.byref(self.solver), max_scenes, max_particles, max_cells, C.byref(h)),
+               "pbf_batch_create")
+        self._h = h
+        self._n = {}
+
+    @staticmethod
+    def device_bytes(solver: Params, max_scenes: int, max_particles: int, max_cells: int) -> int:
+        return int(lib().pbf_batch_device_bytes(C.byref(solver), max_scenes, max_particles, max_cells))
+
+    def add_scene(self, params: Params, particles: np.ndarray) -> int:
+        ps = np.ascontiguousarray(particles, PARTICLE_DTYPE)
+        sid = C.c_uint32()
+        _check(lib().pbf_batch_add_scene(self._h, C.byref(params), _ptr(ps), int(ps.shape[0]), C.byref(sid)),
+               "pbf_batch_add_scene")
+        self._n[sid.value] = int(ps.shape[0])
+        return sid.value
+
+    def remove_scene(self, scene_id: int):
+        _check(lib().pbf_batch_remove_scene(self._h, scene_id), "pbf_batch_remove_scene")
+        self._n.pop(scene_id, None)
+
+    def step(self, nsteps: int = 1, sync: bool = True):
+        _check(lib().pbf_batch_step(self._h, nsteps), "pbf_batch_step")
+        if sync:
+            self.sync()
+
+    def sync(self):
+        _check(lib().pbf_batch_sync(self._h), "pbf_batch_sync")
+
+    def dump_scene(self, scene_id: int):
+        n = self._n.get(scene_id)
+        if n is None:
+            raise PbfError(ERR_NOT_FOUND, "pbf_batch_dump_scene")
+        pos = np.zeros((n, 4), np.float32)
+        vel = np.zeros((n, 4), np.float32)
+        _check(lib().pbf_batch_dump_scene(self._h, scene_id, _ptr(pos), _ptr(vel)), "pbf_batch_dump_scene")
+        return pos, vel
+
+    def set_wave(self, scene_id: int, value: float):
+        _check(lib().pbf_batch_set_wave(self._h, scene_id, float(value)), "pbf_batch_set_wave")
+
+    def info(self):
+        """(scenes, particles, cells) currently held."""
+        s, p, c = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        _check(lib().pbf_batch_info(self._h, C.byref(s), C.byref(p), C.byref(c)), "pbf_batch_info")
+        return s.value, p.value, c.value
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(lib().pbf_batch_get_stream(self._h, C.byref(s)), "pbf_batch_get_stream")
+        return s.value or 0
+
+    def launches_per_step(self) -> int:
+        n = C.c_uint32()
+        _check(lib().pbf_batch_launches_per_step(self._h, C.byref(n)), "pbf_batch_launches_per_step")
+        return n.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().pbf_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 # ------------------------------------------------------------------ operators

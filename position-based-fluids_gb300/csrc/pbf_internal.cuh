@@ -128,16 +128,26 @@ struct DeviceState {
   uint32_t *nbr_cnt = nullptr;         // neighbour counts (paper)
   uint32_t *sort_scratch = nullptr;
   uint32_t *err = nullptr;             // device error flag word
-  SceneDesc *scenes = nullptr;         // device scene table (1 entry)
+  SceneDesc *scenes = nullptr;         // device scene table
   float4 *io_pos = nullptr, *io_vel = nullptr; // input-order staging
+  // batches only (null / 1 for a single scene)
+  uint16_t *sid = nullptr;             // scene of each sorted slot
+  uint32_t *tile_base = nullptr;       // first gather tile of each scene (+ total)
+  uint32_t nscenes = 1;
 };
+
+// Fills dst[0, n) with `value`.
+cudaError_t fill_u16(uint16_t *dst, uint32_t n, uint16_t value, cudaStream_t st);
+// dst[i] = i for i in [0, n).
+cudaError_t iota_range(uint32_t *dst, uint32_t n, cudaStream_t st);
 
 // ------------------------------------------------------- paper-mode launches
 // Raises the dynamic shared-memory limit of the gather kernels (once per
 // process and device, before the first launch).
 cudaError_t paper_configure();
-// Tiles (CTAs) of the gather passes for n particles.
+// Tiles (CTAs) of the gather passes for n particles of one scene.
 uint32_t paper_tiles(uint32_t n);
+uint32_t paper_scene_tiles(uint32_t n_scene);
 cudaError_t paper_predict_hash(const float4 *X, const float4 *V, uint32_t n,
                                const PaperConsts &c, const SceneDesc *scenes,
                                const uint16_t *sid, uint32_t *keys,

@@ -64,6 +64,10 @@ struct NbrCtx {
   const float4 *__restrict__ V2;
   const SceneDesc *__restrict__ scenes;
   const uint16_t *__restrict__ sid;
+  // Batches: first tile of each scene (nscenes + 1 entries); tiles never
+  // straddle scenes.  Null for a single scene.
+  const uint32_t *__restrict__ tile_base;
+  uint32_t nscenes;
   uint32_t *err;
   uint32_t n, maxn;
   float dt, h2;
@@ -76,6 +80,7 @@ struct Ranges {
   uint32_t row_a, nparts, xa[2], xb[2];
   uint32_t listed;   // 1: lists encode this tile's neighbours; 0: fallback
   uint32_t scene;
+  uint32_t k0, k1;   // first and last particle of the tile
 };
 
 __device__ __forceinline__ const SceneDesc &scene_of(const SceneDesc *scenes,
@@ -95,10 +100,30 @@ __host__ __device__ __forceinline__ uint32_t gather_tiles(uint32_t n) {
 // a step computes the same result (it depends only on the sort).  Returns
 // false, uniformly, for a tile past the end.
 __device__ __forceinline__ bool ranges_setup(Ranges &w, uint32_t tile, const NbrCtx &c) {
-  const uint32_t k0 = tile * (uint32_t)kTile;
-  if (k0 >= c.n) return false;
-  const uint32_t k1 = min(k0 + (uint32_t)kTile, c.n) - 1u;
+  // Tile -> particles.  In a batch, tiles are numbered scene by scene and
+  // start at the scene's first particle, so a scene's tiles are the same
+  // alone and in any mix.
+  uint32_t k0, kend;
+  if (c.tile_base) {
+    if (tile >= __ldg(&c.tile_base[c.nscenes])) return false;
+    uint32_t lo = 0, hi = c.nscenes - 1;  // largest s with tile_base[s] <= tile
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1) >> 1;
+      if (__ldg(&c.tile_base[mid]) <= tile) lo = mid;
+      else hi = mid - 1;
+    }
+    const SceneDesc &s = c.scenes[lo];
+    k0 = s.p_begin + (tile - __ldg(&c.tile_base[lo])) * (uint32_t)kTile;
+    kend = s.p_end;
+  } else {
+    k0 = tile * (uint32_t)kTile;
+    kend = c.n;
+  }
+  if (k0 >= kend) return false;
+  const uint32_t k1 = min(k0 + (uint32_t)kTile, kend) - 1u;
   if (threadIdx.x == 0) {
+    w.k0 = k0;
+    w.k1 = k1;
     const uint32_t s0 = c.sid ? c.sid[k0] : 0u;
     const uint32_t s1 = c.sid ? c.sid[k1] : 0u;
     const SceneDesc &sc = c.scenes[s0];
@@ -398,8 +423,8 @@ __global__ void __launch_bounds__(kTile)
                  float4 *__restrict__ Q, float *__restrict__ R) {
   __shared__ Ranges w;
   if (!ranges_setup(w, blockIdx.x, nc)) return;
-  const uint32_t k = blockIdx.x * kTile + threadIdx.x;
-  if (k >= c.n) return;
+  const uint32_t k = w.k0 + threadIdx.x;
+  if (k > w.k1) return;
   const bool listed = w.listed != 0;
   const SceneDesc &sc = nc.scenes[w.scene];
   const float4 pk = P[k];
@@ -432,8 +457,8 @@ __global__ void __launch_bounds__(kTile)
              float4 *__restrict__ Q, float *__restrict__ R) {
   __shared__ Ranges w;
   if (!ranges_setup(w, blockIdx.x, nc)) return;
-  const uint32_t k = blockIdx.x * kTile + threadIdx.x;
-  if (k >= c.n) return;
+  const uint32_t k = w.k0 + threadIdx.x;
+  if (k > w.k1) return;
   const float4 pk = P[k];
   LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
   visit_neighbours(
@@ -453,8 +478,8 @@ __global__ void __launch_bounds__(kTile)
             const float *__restrict__ R, float4 *__restrict__ U, int last) {
   __shared__ Ranges w;
   if (!ranges_setup(w, blockIdx.x, nc)) return;
-  const uint32_t k = blockIdx.x * kTile + threadIdx.x;
-  if (k >= c.n) return;
+  const uint32_t k = w.k0 + threadIdx.x;
+  if (k > w.k1) return;
   const float4 qk = Q[k];
   float sx = 0.f, sy = 0.f, sz = 0.f;
   visit_neighbours(
@@ -497,8 +522,8 @@ __global__ void __launch_bounds__(kTile)
                 float4 *__restrict__ PW) {
   __shared__ Ranges w;
   if (!ranges_setup(w, blockIdx.x, nc)) return;
-  const uint32_t k = blockIdx.x * kTile + threadIdx.x;
-  if (k >= c.n) return;
+  const uint32_t k = w.k0 + threadIdx.x;
+  if (k > w.k1) return;
   const float4 pk = P[k];
   const float4 uk = U[k];
   float wx = 0.f, wy = 0.f, wz = 0.f;
@@ -533,8 +558,8 @@ __global__ void __launch_bounds__(kTile)
                   float4 *__restrict__ V, uint32_t *__restrict__ ID) {
   __shared__ Ranges w;
   if (!ranges_setup(w, blockIdx.x, nc)) return;
-  const uint32_t k = blockIdx.x * kTile + threadIdx.x;
-  if (k >= c.n) return;
+  const uint32_t k = w.k0 + threadIdx.x;
+  if (k > w.k1) return;
   const float4 pk = PW[k];
   const float4 uk = U[k];
   const float4 wk = Wv[k];
@@ -616,6 +641,11 @@ __global__ void k_iota(uint32_t *__restrict__ dst, uint32_t n) {
   if (k < n) dst[k] = k;
 }
 
+__global__ void k_fill_u16(uint16_t *__restrict__ dst, uint32_t n, uint16_t value) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[k] = value;
+}
+
 inline uint32_t blocks_for(uint64_t n, uint32_t t) {
   return (uint32_t)((n + t - 1) / t);
 }
@@ -630,6 +660,8 @@ NbrCtx make_ctx(const DeviceState &d, const PaperConsts &c, const uint16_t *sid)
   nc.V2 = d.V2;
   nc.scenes = d.scenes;
   nc.sid = sid;
+  nc.tile_base = d.tile_base;
+  nc.nscenes = d.nscenes;
   nc.err = d.err;
   nc.n = c.n;
   nc.maxn = c.maxn;
@@ -723,5 +755,18 @@ cudaError_t iota_u32(uint32_t *dst, uint32_t n, cudaStream_t st) {
   k_iota<<<blocks_for(n, 256), 256, 0, st>>>(dst, n);
   return cudaGetLastError();
 }
+
+cudaError_t iota_range(uint32_t *dst, uint32_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  return iota_u32(dst, n, st);
+}
+
+cudaError_t fill_u16(uint16_t *dst, uint32_t n, uint16_t value, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_fill_u16<<<blocks_for(n, 256), 256, 0, st>>>(dst, n, value);
+  return cudaGetLastError();
+}
+
+uint32_t paper_scene_tiles(uint32_t n_scene) { return gather_tiles(n_scene); }
 
 }  // namespace pbf

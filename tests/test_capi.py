@@ -187,6 +187,23 @@ def test_create_validation(pbf):
     s.close()
 
 
+def test_batch_host_checks(pbf):
+    """Batch arguments rejected before any device work."""
+    sc = pbf.scenes.config_small()
+    ref = sc.params.copy()
+    ref.mode = pbf.MODE_REF_COMPAT
+    for args in ((ref, 4, 1000, 1000), (sc.params, 0, 1000, 1000), (sc.params, 70000, 1000, 1000),
+                 (sc.params, 4, 0, 1000), (sc.params, 4, 1000, 0)):
+        with pytest.raises(pbf.PbfError) as e:
+            pbf.Batch(*args)
+        assert e.value.status == pbf.ERR_INVALID
+    small = pbf.Batch.device_bytes(sc.params, 4, 1 << 16, 1 << 16)
+    big = pbf.Batch.device_bytes(sc.params, 256, 16 << 20, 16 << 20)
+    assert 0 < small < big
+    # a 16M-particle batch stays well inside one GB300
+    assert big < 16 * (1 << 30)
+
+
 def test_scenes_shapes(pbf):
     s1 = pbf.scenes.config_small()
     assert s1.n == 32768 and s1.params.ncells == 16 * 16 * 32
