@@ -254,6 +254,66 @@ int pbf_batch_get_stream(const pbf_batch *b, void **stream);
 int pbf_batch_launches_per_step(const pbf_batch *b, uint32_t *launches);
 int pbf_batch_destroy(pbf_batch *b);
 
+/* ------------------------------------------------------- served scenes */
+/* A request loop over one batch (continuous batching).  Requests (a scene
+ * and a step count) are queued by pbf_server_submit; pbf_server_poll
+ * retires the requests whose steps are done (their final state is copied to
+ * host memory held by the server), admits queued requests in arrival order
+ * while they fit the batch (first fit: a request that does not fit yet does
+ * not hold back smaller ones behind it), and enqueues the next chunk of
+ * batched steps.  A chunk is at most `max_chunk` steps and never longer than
+ * the fewest steps any active request still needs, so every request runs
+ * exactly its own step count.  The batch's capacities are derived from an
+ * HBM budget at creation and allocated once; admission never allocates.
+ * A request's result is bitwise the same as the scene run alone.
+ * No reference counterpart (the reference runs one scene per process). */
+typedef struct pbf_server pbf_server;
+
+typedef enum pbf_request_state {
+  PBF_REQ_QUEUED = 0,
+  PBF_REQ_ACTIVE = 1,
+  PBF_REQ_DONE = 2
+} pbf_request_state;
+
+typedef struct pbf_server_stats {
+  uint64_t submitted, admitted, completed;
+  uint64_t batch_steps;          /* batched steps enqueued                */
+  uint64_t particle_steps;       /* sum over steps of active particles    */
+  uint32_t queued, active;       /* requests now waiting / on the device  */
+  uint32_t active_particles, active_cells;
+  uint32_t max_particles, max_cells, max_scenes; /* capacities            */
+  uint32_t pad_;
+  uint64_t device_bytes;         /* bytes the batch allocated             */
+  uint64_t launches;             /* kernel launches enqueued              */
+} pbf_server_stats;
+
+/* Creates a server whose batch fits `hbm_budget_bytes` of device memory.
+ * Cells are budgeted at `cells_per_particle` per particle slot (at least 1).
+ * PBF_ERR_BUDGET if the budget holds no useful batch. */
+int pbf_server_create(const pbf_params *solver, uint64_t hbm_budget_bytes,
+                      uint32_t max_scenes, float cells_per_particle,
+                      uint32_t max_chunk, pbf_server **out);
+/* Queues a request (the particles are copied).  PBF_ERR_BUDGET if the
+ * scene alone exceeds the server's capacities. */
+int pbf_server_submit(pbf_server *s, const pbf_params *scene,
+                      const pbf_particle *particles, uint32_t n,
+                      uint32_t steps, uint64_t *request_id);
+/* One turn of the loop.  With `wait` = 0 it returns at once while a chunk
+ * is still running (*ncompleted = 0); with `wait` = 1 it first waits for the
+ * running chunk.  Ids of requests completed in this turn are written to
+ * completed[0 .. min(*ncompleted, cap)).  *busy is set to 1 while requests
+ * remain queued or active. */
+int pbf_server_poll(pbf_server *s, int wait, uint64_t *completed, uint32_t cap,
+                    uint32_t *ncompleted, int *busy);
+int pbf_server_request_info(const pbf_server *s, uint64_t request_id,
+                            int *state, uint32_t *n, uint32_t *steps_done);
+/* Copies a completed request's final state (dumpData layout) and releases
+ * it.  PBF_ERR_STATE if it is not done, PBF_ERR_NOT_FOUND if unknown. */
+int pbf_server_result(pbf_server *s, uint64_t request_id, float *pos4,
+                      float *vel4);
+int pbf_server_stats_get(const pbf_server *s, pbf_server_stats *out);
+int pbf_server_destroy(pbf_server *s);
+
 /* ------------------------------------ neighbour-structure operators (L4) */
 /* Cell hash of N predicted positions (float4, .w ignored) on the grid of
  * `params` (update_cells.cl:10-15 / calc_hash.cl:15-20).  Each axis cell

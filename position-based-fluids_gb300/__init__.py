@@ -8,7 +8,9 @@ mirrors the reference's host interface (MrMagne/position-based-fluids):
   dumpData, getters, setWaveGenerator);
 * ``read_config`` / ``read_particles`` / ``data_path`` -- ConfigReader,
   PartReader and DataLoader (``src/io/*``, ``src/DataLoader.*``);
-* ``op_*`` -- the neighbour-structure operators on device pointers.
+* ``op_*`` -- the neighbour-structure operators on device pointers;
+* ``Batch`` / ``Server`` -- many scenes per step, and the request loop over
+  them (no reference counterpart).
 
 There is no CPU fallback: if the library is missing, importing this package
 raises.
@@ -36,6 +38,10 @@ ERR_IO = 5
 ERR_BUDGET = 6
 ERR_STATE = 7
 ERR_NOT_FOUND = 8
+
+REQ_QUEUED = 0
+REQ_ACTIVE = 1
+REQ_DONE = 2
 
 
 class Params(C.Structure):
@@ -91,6 +97,21 @@ class Particle(C.Structure):
 PARTICLE_DTYPE = np.dtype([("m", np.float32), ("x", np.float32, 3), ("v", np.float32, 3),
                            ("a", np.float32, 3)])
 assert PARTICLE_DTYPE.itemsize == C.sizeof(Particle)
+
+
+class ServerStats(C.Structure):
+    """pbf_server_stats."""
+
+    _fields_ = [("submitted", C.c_uint64), ("admitted", C.c_uint64), ("completed", C.c_uint64),
+                ("batch_steps", C.c_uint64), ("particle_steps", C.c_uint64),
+                ("queued", C.c_uint32), ("active", C.c_uint32),
+                ("active_particles", C.c_uint32), ("active_cells", C.c_uint32),
+                ("max_particles", C.c_uint32), ("max_cells", C.c_uint32), ("max_scenes", C.c_uint32),
+                ("pad_", C.c_uint32), ("device_bytes", C.c_uint64), ("launches", C.c_uint64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad_"}
+
 
 _lib = None
 
@@ -167,6 +188,14 @@ def lib():
             "pbf_batch_get_stream": ([vp, C.POINTER(vp)], i32),
             "pbf_batch_launches_per_step": ([vp, C.POINTER(u32)], i32),
             "pbf_batch_destroy": ([vp], i32),
+            "pbf_server_create": ([pp, C.c_uint64, u32, f32, u32, C.POINTER(vp)], i32),
+            "pbf_server_submit": ([vp, pp, vp, u32, u32, C.POINTER(C.c_uint64)], i32),
+            "pbf_server_poll": ([vp, i32, vp, u32, C.POINTER(u32), C.POINTER(i32)], i32),
+            "pbf_server_request_info": ([vp, C.c_uint64, C.POINTER(i32), C.POINTER(u32), C.POINTER(u32)],
+                                        i32),
+            "pbf_server_result": ([vp, C.c_uint64, vp, vp], i32),
+            "pbf_server_stats_get": ([vp, C.POINTER(ServerStats)], i32),
+            "pbf_server_destroy": ([vp], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -456,6 +485,82 @@ class Batch:
     def close(self):
         if getattr(self, "_h", None):
             lib().pbf_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Server:
+    """Served scenes (pbf_server_* in include/pbf.h): a request loop with
+    continuous batching over one batch sized by an HBM budget."""
+
+    def __init__(self, solver: Params, hbm_budget_bytes: int, max_scenes: int = 1024,
+                 cells_per_particle: float = 2.0, max_chunk: int = 16):
+        self.solver = solver.copy()
+        h = C.c_void_p()
+        _check(lib().pbf_server_create(C.byref(self.solver), int(hbm_budget_bytes), max_scenes,
+                                       float(cells_per_particle), max_chunk, C.byref(h)), "pbf_server_create")
+        self._h = h
+        self._n = {}
+        self._ids = (C.c_uint64 * 4096)()
+
+    def submit(self, params: Params, particles: np.ndarray, steps: int) -> int:
+        ps = np.ascontiguousarray(particles, PARTICLE_DTYPE)
+        rid = C.c_uint64()
+        _check(lib().pbf_server_submit(self._h, C.byref(params), _ptr(ps), int(ps.shape[0]), int(steps),
+                                       C.byref(rid)), "pbf_server_submit")
+        self._n[rid.value] = int(ps.shape[0])
+        return rid.value
+
+    def poll(self, wait: bool = False):
+        """One turn of the loop: (ids completed in this turn, busy)."""
+        cnt = C.c_uint32()
+        busy = C.c_int()
+        _check(lib().pbf_server_poll(self._h, int(wait), self._ids, len(self._ids), C.byref(cnt),
+                                     C.byref(busy)), "pbf_server_poll")
+        return [self._ids[i] for i in range(min(cnt.value, len(self._ids)))], bool(busy.value)
+
+    def run_until_idle(self):
+        done = []
+        busy = True
+        while busy:
+            ids, busy = self.poll(wait=True)
+            done += ids
+        return done
+
+    def info(self, rid: int):
+        """(state, particles, steps done) of a request."""
+        st, n, k = C.c_int(), C.c_uint32(), C.c_uint32()
+        _check(lib().pbf_server_request_info(self._h, rid, C.byref(st), C.byref(n), C.byref(k)),
+               "pbf_server_request_info")
+        return st.value, n.value, k.value
+
+    def result(self, rid: int):
+        n = self._n.get(rid, 1)
+        pos = np.zeros((n, 4), np.float32)
+        vel = np.zeros((n, 4), np.float32)
+        _check(lib().pbf_server_result(self._h, rid, _ptr(pos), _ptr(vel)), "pbf_server_result")
+        self._n.pop(rid, None)
+        return pos, vel
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(lib().pbf_server_stats_get(self._h, C.byref(st)), "pbf_server_stats_get")
+        return st.as_dict()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().pbf_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -161,6 +161,46 @@ int launch_batch_step(pbf_batch *b) {
 
 }  // namespace
 
+namespace pbf {
+
+int batch_check_scene(const pbf_batch *b, const pbf_params &scene, uint32_t n,
+                      pbf_params *merged_out, uint64_t *cells_out) {
+  // The batch's solver settings with this scene's box, grid and walls.
+  pbf_params merged = b->solver;
+  merged.x_min = scene.x_min; merged.x_max = scene.x_max;
+  merged.y_min = scene.y_min; merged.y_max = scene.y_max;
+  merged.z_min = scene.z_min; merged.z_max = scene.z_max;
+  merged.x_n = scene.x_n; merged.y_n = scene.y_n; merged.z_n = scene.z_n;
+  merged.wall_margin = scene.wall_margin;
+  {
+    const int v = validate_params(merged, n);
+    if (v != PBF_OK) return v;
+  }
+  const float h = params_h(b->solver);
+  const float ext[3] = {merged.x_max - merged.x_min, merged.y_max - merged.y_min,
+                        merged.z_max - merged.z_min};
+  const float nc[3] = {merged.x_n, merged.y_n, merged.z_n};
+  for (int a = 0; a < 3; ++a)
+    if (ext[a] / nc[a] < h * (1.0f - 1e-5f)) {
+      set_error_message("scene cells must be at least the batch's h long");
+      return PBF_ERR_INVALID;
+    }
+  // Clamp bounds from this scene's box; wall margin default from the batch h.
+  merged.wall_margin = scene.wall_margin < 0.0f ? 0.25f * h : scene.wall_margin;
+  if (merged_out) *merged_out = merged;
+  if (cells_out) *cells_out = grid_cells(merged);
+  return PBF_OK;
+}
+
+void batch_capacity(const pbf_batch *b, uint32_t *scenes, uint32_t *particles,
+                    uint32_t *cells) {
+  *scenes = b->max_scenes;
+  *particles = b->max_particles;
+  *cells = b->max_cells;
+}
+
+}  // namespace pbf
+
 extern "C" {
 
 size_t pbf_batch_device_bytes(const pbf_params *solver, uint32_t max_scenes,
@@ -235,30 +275,13 @@ int pbf_batch_create(const pbf_params *solver, uint32_t max_scenes, uint32_t max
   return PBF_OK;
 }
 
+
 int pbf_batch_add_scene(pbf_batch *b, const pbf_params *scene, const pbf_particle *particles,
                         uint32_t n, uint32_t *scene_id) {
   if (!b || !scene || !particles || !scene_id || n == 0) return PBF_ERR_INVALID;
-  // The batch's solver settings with this scene's box, grid and walls.
-  pbf_params merged = b->solver;
-  merged.x_min = scene->x_min; merged.x_max = scene->x_max;
-  merged.y_min = scene->y_min; merged.y_max = scene->y_max;
-  merged.z_min = scene->z_min; merged.z_max = scene->z_max;
-  merged.x_n = scene->x_n; merged.y_n = scene->y_n; merged.z_n = scene->z_n;
-  merged.wall_margin = scene->wall_margin;
-  {
-    const int v = validate_params(merged, n);
-    if (v != PBF_OK) return v;
-  }
-  const float h = params_h(b->solver);
-  const float ext[3] = {merged.x_max - merged.x_min, merged.y_max - merged.y_min,
-                        merged.z_max - merged.z_min};
-  const float nc[3] = {merged.x_n, merged.y_n, merged.z_n};
-  for (int a = 0; a < 3; ++a)
-    if (ext[a] / nc[a] < h * (1.0f - 1e-5f)) {
-      set_error_message("scene cells must be at least the batch's h long");
-      return PBF_ERR_INVALID;
-    }
-  const uint64_t cells = grid_cells(merged);
+  pbf_params merged;
+  uint64_t cells = 0;
+  PBF_TRY_STATUS(batch_check_scene(b, *scene, n, &merged, &cells));
   if (b->scenes.size() + 1 > b->max_scenes || (uint64_t)b->n_total + n > b->max_particles ||
       (uint64_t)b->cells_total + cells > b->max_cells) {
     set_error_message("batch capacity exceeded");
@@ -268,8 +291,6 @@ int pbf_batch_add_scene(pbf_batch *b, const pbf_params *scene, const pbf_particl
   rec.id = b->next_id++;
   rec.n = n;
   rec.cells = (uint32_t)cells;
-  // Clamp bounds from this scene's box; wall margin default from the batch h.
-  merged.wall_margin = scene->wall_margin < 0.0f ? 0.25f * h : scene->wall_margin;
   rec.desc = make_scene(merged);
   const uint32_t p0 = b->n_total;
   std::vector<float4> pos(n), vel(n);

@@ -31,4 +31,12 @@ SceneDesc make_scene(const pbf_params &p);
 int validate_params(const pbf_params &p, uint32_t n);
 uint64_t grid_cells(const pbf_params &p);
 
+// Checks a scene for a batch (grid, cell lengths against the batch's h) and
+// returns the batch's solver settings with the scene's box, grid and walls,
+// and the scene's cell count.  No capacity check.
+int batch_check_scene(const pbf_batch *b, const pbf_params &scene, uint32_t n,
+                      pbf_params *merged, uint64_t *cells);
+void batch_capacity(const pbf_batch *b, uint32_t *scenes, uint32_t *particles,
+                    uint32_t *cells);
+
 }  // namespace pbf

@@ -104,6 +104,25 @@ def config_4m(seed: int = SEED) -> Scene:
                   "origins": [[m, m, m], [bx, m, m]], "seed": seed})
 
 
+def block_in_double_box(dims, seed: int, steps: int, name: str) -> Scene:
+    """A dam-break block in the corner of a box twice the block's extent on
+    every axis (rounded up to whole cells of size h)."""
+    ext = [(d - 1) * SPACING + 2 * 0.25 * H for d in dims]
+    cells = tuple(max(1, int(math.ceil(2 * e / H))) for e in ext)
+    box = tuple(c * H for c in cells)
+    p = base_params(box, cells)
+    m = 0.25 * H
+    ps = block((m, m, m), dims, seed)
+    return Scene(name, p, ps, steps, {"block": list(dims), "box": list(box), "cells": list(cells),
+                                      "seed": seed})
+
+
+def _dims_for(n_target: float, ax: float, az: float):
+    # block dims proportional to (ax, 1, az) with product ~ n_target
+    base = (n_target / (ax * az)) ** (1.0 / 3.0)
+    return tuple(max(2, int(round(v))) for v in (base * ax, base, base * az))
+
+
 def mixed_batch(count: int = 256, n_min: int = 4096, n_max: int = 262144, seed: int = SEED) -> list[Scene]:
     """Independent dam breaks with log-uniform particle counts and block
     aspect ratios in [0.5, 2]; each box is twice the block extent."""
@@ -112,15 +131,43 @@ def mixed_batch(count: int = 256, n_min: int = 4096, n_max: int = 262144, seed: 
     for s in range(count):
         n_target = math.exp(rng.uniform(math.log(n_min), math.log(n_max)))
         ax, az = rng.uniform(0.5, 2.0, size=2)
-        # block dims proportional to (ax, 1, az) with product ~ n_target
-        base = (n_target / (ax * az)) ** (1.0 / 3.0)
-        dims = tuple(max(2, int(round(v))) for v in (base * ax, base, base * az))
-        ext = [(d - 1) * SPACING + 2 * 0.25 * H for d in dims]
-        cells = tuple(max(1, int(math.ceil(2 * e / H))) for e in ext)
-        box = tuple(c * H for c in cells)
-        p = base_params(box, cells)
-        m = 0.25 * H
-        ps = block((m, m, m), dims, seed + 1000 + s)
-        scenes.append(Scene(f"batch_{s}", p, ps, 300, {"block": list(dims), "box": list(box),
-                                                        "cells": list(cells)}))
+        scenes.append(block_in_double_box(_dims_for(n_target, ax, az), seed + 1000 + s, 300, f"batch_{s}"))
     return scenes
+
+
+@dataclass
+class Request:
+    """One served scene solve: arrival time (s from the start of the stream),
+    block dims, step count and seed; `scene()` builds the particles."""
+    index: int
+    arrival: float
+    dims: tuple
+    steps: int
+    seed: int
+
+    @property
+    def n(self) -> int:
+        return int(np.prod(self.dims))
+
+    def scene(self) -> Scene:
+        return block_in_double_box(self.dims, self.seed, self.steps, f"request_{self.index}")
+
+
+def request_stream(duration_s: float, rate: float = 50.0, n_min: int = 8192, n_max: int = 524288,
+                   steps_min: int = 100, steps_max: int = 1000, seed: int = SEED) -> list[Request]:
+    """A seeded Poisson stream of dam-break solves: exponential inter-arrival
+    times of mean 1/rate, N log-uniform in [n_min, n_max], block aspect
+    ratios uniform in [0.5, 2], step counts uniform in {steps_min..steps_max}."""
+    rng = np.random.default_rng(seed + 7)
+    out = []
+    t = 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration_s:
+            break
+        n_target = math.exp(rng.uniform(math.log(n_min), math.log(n_max)))
+        ax, az = rng.uniform(0.5, 2.0, size=2)
+        steps = int(rng.integers(steps_min, steps_max + 1))
+        i = len(out)
+        out.append(Request(i, t, _dims_for(n_target, ax, az), steps, seed + 5000 + i))
+    return out

@@ -202,6 +202,15 @@ def test_batch_host_checks(pbf):
     assert 0 < small < big
     # a 16M-particle batch stays well inside one GB300
     assert big < 16 * (1 << 30)
+    # server arguments and budgets that hold no batch
+    for args, kw in (((sc.params, 1 << 30), {"max_scenes": 0}), ((sc.params, 1 << 30), {"max_chunk": 0}),
+                     ((sc.params, 1 << 30), {"cells_per_particle": 0.5}), ((ref, 1 << 30), {})):
+        with pytest.raises(pbf.PbfError) as e:
+            pbf.Server(*args, **kw)
+        assert e.value.status == pbf.ERR_INVALID
+    with pytest.raises(pbf.PbfError) as e:
+        pbf.Server(sc.params, 1 << 16)
+    assert e.value.status == pbf.ERR_BUDGET
 
 
 def test_scenes_shapes(pbf):
