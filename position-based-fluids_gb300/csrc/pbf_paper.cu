@@ -25,16 +25,17 @@
 // current positions with W = 0 beyond h.
 //
 // Gather passes work on tiles of kTile consecutive sorted particles, one
-// thread each.  Sorted by cell key, a tile's particles sit in one or two
-// x-rows of the grid; the 27-cell neighbourhoods of each row's share lie in
-// 9 row ranges (the share's x span widened by one cell, in the rows y-1..y+1,
-// z-1..z+1), which are contiguous slot ranges of the sorted arrays: 18
-// ranges at most.  Neighbour lists store each neighbour as 16 bits, the
-// range (5 bits) and the offset inside it (11 bits), eight per 16-byte word:
+// thread each.  Sorted by cell key, a tile's particles sit in a few
+// consecutive x-rows of the grid; the 27-cell neighbourhoods of each row's
+// share lie in 9 row ranges (the share's x span widened by one cell, in the
+// rows y-1..y+1, z-1..z+1), which are contiguous slot ranges of the sorted
+// arrays: 27 ranges for a tile of at most kMaxParts = 3 rows.  Neighbour
+// lists store each neighbour as 16 bits, the range (5 bits) and the offset
+// inside it (11 bits), eight per 16-byte word:
 // group g of particle k is nbr4[g*N + k], so a warp reads its particles' next
-// eight neighbours with one coalesced load per thread, and the eight
-// neighbour loads that follow are independent.  A tile spanning more than
-// two rows (sparse regions) or two scenes, a range longer than 2048 slots,
+// eight neighbours with one coalesced load per thread, and the neighbour
+// loads that follow are independent.  A tile spanning more than
+// three rows (sparse regions) or two scenes, a range longer than 2048 slots,
 // and a particle whose set exceeds the list capacity re-derive the set from
 // the cells and the step-start positions in every pass instead (same order,
 // same arithmetic).
@@ -54,6 +55,7 @@ namespace {
 constexpr int kTile = 128;          // particles (threads) per gather CTA
 constexpr uint32_t kRelBits = 11;   // offset bits of a list entry
 constexpr uint32_t kRelMax = 1u << kRelBits;
+constexpr uint32_t kMaxParts = 3;   // x-rows a listed tile may span
 
 struct NbrCtx {
   const uint4 *__restrict__ nbr4;
@@ -75,9 +77,9 @@ struct NbrCtx {
 
 // Per-CTA description of the tile's neighbourhood ranges.
 struct Ranges {
-  uint32_t S[32];    // first slot of each row range (18 used)
+  uint32_t S[32];    // first slot of each row range (9 per part)
   uint32_t len[32];  // slots in each row range
-  uint32_t row_a, nparts, xa[2], xb[2];
+  uint32_t row_a, nparts, xa[kMaxParts], xb[kMaxParts];
   uint32_t listed;   // 1: lists encode this tile's neighbours; 0: fallback
   uint32_t scene;
   uint32_t k0, k1;   // first and last particle of the tile
@@ -95,8 +97,8 @@ __host__ __device__ __forceinline__ uint32_t gather_tiles(uint32_t n) {
 
 // Computes the row ranges of tile `tile` (particles [tile*kTile, +kTile)):
 // range 9*part + (dz+1)*3 + (dy+1) covers, in row (y+dy, z+dz), the cells
-// x in [xa-1, xb+1] clipped to the row, where part 0/1 is the tile's first/
-// second row and [xa, xb] the x span of its particles there.  Every pass of
+// x in [xa-1, xb+1] clipped to the row, where part p is the tile's (p+1)-th
+// row and [xa, xb] the x span of its particles there.  Every pass of
 // a step computes the same result (it depends only on the sort).  Returns
 // false, uniformly, for a tile past the end.
 __device__ __forceinline__ bool ranges_setup(Ranges &w, uint32_t tile, const NbrCtx &c) {
@@ -132,17 +134,17 @@ __device__ __forceinline__ bool ranges_setup(Ranges &w, uint32_t tile, const Nbr
     const uint32_t ra = a / nx, rb = b / nx;
     w.scene = s0;
     w.row_a = ra;
-    w.nparts = (s0 == s1 && rb >= ra && rb <= ra + 1u) ? (rb - ra + 1u) : 0u;
-    w.xa[0] = a % nx;
-    w.xb[0] = rb == ra ? b % nx : nx - 1u;
-    w.xa[1] = 0;
-    w.xb[1] = b % nx;
+    w.nparts = (s0 == s1 && rb >= ra && rb < ra + kMaxParts) ? (rb - ra + 1u) : 0u;
+    for (uint32_t p = 0; p < kMaxParts; ++p) {
+      w.xa[p] = p == 0 ? a % nx : 0u;
+      w.xb[p] = ra + p == rb ? b % nx : nx - 1u;
+    }
   }
   __syncthreads();
   if (threadIdx.x < 32) {
     const uint32_t t = threadIdx.x, part = t / 9u, q = t % 9u;
     uint32_t S = 0, L = 0;
-    if (t < 18 && part < w.nparts) {
+    if (t < 9u * kMaxParts && part < w.nparts) {
       const SceneDesc &sc = c.scenes[w.scene];
       const uint32_t nx = (uint32_t)sc.ncell[0], ny = (uint32_t)sc.ncell[1], nz = (uint32_t)sc.ncell[2];
       const uint32_t row = w.row_a + part;
@@ -174,10 +176,12 @@ __device__ __forceinline__ uint32_t entry_slot(const Ranges &w, uint32_t e, uint
   return min(w.S[(e >> kRelBits) & 31u] + (e & (kRelMax - 1u)), n - 1u);
 }
 
-// For the `cnt` listed neighbours of particle k: per group of eight, first
-// load(slot) for all eight (unconditionally; past-the-end entries read a
-// valid slot), then f(data, valid) for each -- so that the eight gathers are
-// in flight together instead of one after another.
+// For the `cnt` listed neighbours of particle k: per half group of four,
+// first load(slot) for all four (unconditionally; past-the-end entries read
+// a valid slot), then f(data, valid) for each -- so that the four gathers
+// are in flight together instead of one after another.  (Four rather than
+// eight: measured on GB300, the smaller batch keeps the lambda and delta-p
+// kernels at 40 registers, 12 CTAs per SM, and runs ~5% faster.)
 template <typename Load, typename F>
 __device__ __forceinline__ void for_each_listed(const NbrCtx &c, const Ranges &w, uint32_t k,
                                                 uint32_t cnt, Load &&load, F &&f) {
@@ -186,12 +190,16 @@ __device__ __forceinline__ void for_each_listed(const NbrCtx &c, const Ranges &w
     const uint4 v = __ldg(&c.nbr4[(size_t)g * c.n + k]);
     const uint32_t rem = cnt - (g << 3);
     const uint32_t words[4] = {v.x, v.y, v.z, v.w};
-    decltype(load(0u)) data[8];
 #pragma unroll
-    for (int e = 0; e < 8; ++e)
-      data[e] = load(entry_slot(w, (words[e >> 1] >> ((e & 1) * 16)) & 0xFFFFu, c.n));
+    for (int h = 0; h < 8; h += 4) {
+      if ((uint32_t)h >= rem) break;
+      decltype(load(0u)) data[4];
 #pragma unroll
-    for (int e = 0; e < 8; ++e) f(data[e], (uint32_t)e < rem);
+      for (int e = 0; e < 4; ++e)
+        data[e] = load(entry_slot(w, (words[(h + e) >> 1] >> (((h + e) & 1) * 16)) & 0xFFFFu, c.n));
+#pragma unroll
+      for (int e = 0; e < 4; ++e) f(data[e], (uint32_t)(h + e) < rem);
+    }
   }
 }
 
@@ -432,14 +440,16 @@ __global__ void __launch_bounds__(kTile)
   ListWriter lw;
   uint32_t cnt = 0;
   const uint32_t key = nc.skeys[k];
-  // Which of the tile's rows (parts) this particle belongs to.
-  const uint32_t part = (key - sc.cell_base) / (uint32_t)sc.ncell[0] == w.row_a ? 0u : 9u;
+  // First range of the tile's row (part) this particle belongs to.
+  const uint32_t part = 9u * ((key - sc.cell_base) / (uint32_t)sc.ncell[0] - w.row_a);
   scan_rows_batched(k, key, sc, nc.off, [&](uint32_t j) { return __ldg(&P[j]); },
                     [&](int q0, uint32_t j, float4 pj, bool valid) {
     const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
     if (valid && r2 > 0.0f && r2 < c.h2) {
-      const uint32_t q = part + (uint32_t)q0;
+      // (part is meaningful for listed tiles only; the clamp keeps the
+      // shared-memory read in bounds for the others)
+      const uint32_t q = min(part + (uint32_t)q0, 31u);
       const uint32_t rel = j - w.S[q];
       if (listed && cnt < c.maxn) lw.put(nbr4, c.n, k, cnt, (q << kRelBits) | (rel & (kRelMax - 1u)));
       ++cnt;
