@@ -5,9 +5,9 @@
 // sorted state and consecutive key ranges [cell_base, cell_base + cells).
 // Because every key of scene s is below every key of scene s+1, the stable
 // sort keeps each scene's particles inside its range, in the order the scene
-// alone would have; the gather tiles are numbered scene by scene from each
-// scene's first particle.  A scene therefore runs exactly the operations it
-// runs alone, whatever else is in the batch.
+// alone would have, and every kernel works on one particle per thread with
+// neighbours from the particle's own scene.  A scene therefore runs exactly
+// the operations it runs alone, whatever else is in the batch.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -42,12 +42,12 @@ struct SceneRec {
 };
 
 size_t bytes_per_particle(uint32_t maxn) {
-  return 9 * sizeof(float4)            // X V X2 V2 P Q D U W
-         + 6 * sizeof(uint32_t)        // ID ID2 keys skeys perm nbr_cnt
-         + sizeof(float)               // R
-         + (size_t)maxn * 2            // lists
-         + sizeof(uint16_t)            // sid
-         + 2 * sizeof(float4);         // io staging
+  return 9 * sizeof(float4)                   // X V X2 V2 P Q D U W
+         + 6 * sizeof(uint32_t)               // ID ID2 keys skeys perm nbr_cnt
+         + sizeof(float)                      // R
+         + (size_t)paper_list_words(maxn) * 16  // lists
+         + sizeof(uint16_t)                   // sid
+         + 2 * sizeof(float4);                // io staging
 }
 
 }  // namespace
@@ -67,7 +67,6 @@ struct pbf_batch {
   bool dirty = true;
   cudaGraphExec_t graph = nullptr;
   std::vector<SceneDesc> table;
-  std::vector<uint32_t> tile_base;
 };
 
 namespace {
@@ -97,36 +96,27 @@ int find_scene(const pbf_batch *b, uint32_t id) {
   return -1;
 }
 
-// Recomputes bases, uploads the scene table, tile table and scene ids.
+// Recomputes bases, uploads the scene table and scene ids.
 int apply_layout(pbf_batch *b) {
   DeviceState &d = b->d;
   b->table.resize(b->scenes.size());
-  b->tile_base.assign(b->scenes.size() + 1, 0);
-  uint32_t p = 0, c = 0, t = 0;
+  uint32_t p = 0, c = 0;
   for (size_t i = 0; i < b->scenes.size(); ++i) {
     SceneRec &s = b->scenes[i];
     s.desc.p_begin = p;
     s.desc.p_end = p + s.n;
     s.desc.cell_base = c;
     b->table[i] = s.desc;
-    b->tile_base[i] = t;
     p += s.n;
     c += s.cells;
-    t += paper_scene_tiles(s.n);
   }
-  b->tile_base[b->scenes.size()] = t;
   b->n_total = p;
   b->cells_total = c;
   b->pc.n = p;
-  b->pc.tiles = t;
-  d.nscenes = (uint32_t)b->scenes.size();
   b->plan = make_sort_plan(p, bits_for(std::max<uint32_t>(c, 1)));
   if (!b->scenes.empty()) {
     PBF_TRY(cudaMemcpyAsync(d.scenes, b->table.data(), b->table.size() * sizeof(SceneDesc),
                             cudaMemcpyHostToDevice, b->stream));
-    PBF_TRY(cudaMemcpyAsync(d.tile_base, b->tile_base.data(),
-                            b->tile_base.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                            b->stream));
     for (size_t i = 0; i < b->scenes.size(); ++i)
       PBF_TRY(fill_u16(d.sid + b->table[i].p_begin, b->scenes[i].n, (uint16_t)i, b->stream));
   }
@@ -210,7 +200,7 @@ size_t pbf_batch_device_bytes(const pbf_params *solver, uint32_t max_scenes,
   const SortPlan plan = make_sort_plan(max_particles, 32);
   return (size_t)max_particles * bytes_per_particle(pc.maxn) +
          ((size_t)max_cells + 1) * sizeof(uint32_t) + plan.words * sizeof(uint32_t) +
-         (size_t)max_scenes * sizeof(SceneDesc) + ((size_t)max_scenes + 1) * sizeof(uint32_t) + 64;
+         (size_t)max_scenes * sizeof(SceneDesc) + 64;
 }
 
 int pbf_batch_create(const pbf_params *solver, uint32_t max_scenes, uint32_t max_particles,
@@ -252,12 +242,11 @@ int pbf_batch_create(const pbf_params *solver, uint32_t max_scenes, uint32_t max
   A(&d.D, M); A(&d.U, M); A(&d.W, M);
   A(&d.ID, M); A(&d.ID2, M); A(&d.keys, M); A(&d.skeys, M); A(&d.perm, M);
   A(&d.nbr_cnt, M); A(&d.R, M); A(&d.sid, M);
-  A(&d.nbr, (size_t)(b->pc.maxn / 8u) * M);
+  A(&d.nbr, (size_t)paper_list_words(b->pc.maxn) * M);
   A(&d.io_pos, M); A(&d.io_vel, M);
   A(&d.offsets, (size_t)max_cells + 1);
   A(&d.sort_scratch, make_sort_plan(max_particles, 32).words);
   A(&d.scenes, max_scenes);
-  A(&d.tile_base, (size_t)max_scenes + 1);
   A(&d.err, 1);
   if (rc != PBF_OK) {
     release(b.get());

@@ -44,7 +44,6 @@ struct PaperConsts {
   int32_t scorr_n3;              // 3 * n
   float xsph_c, vort_eps;
   uint32_t n, maxn;
-  uint32_t tiles;  // cell-block tiles of the gather passes (all scenes)
 };
 
 // The 18 constants the reference bakes into its OpenCL program
@@ -124,16 +123,14 @@ struct DeviceState {
   float *S = nullptr;                  // lambda (ref-compat)
   uint32_t *keys = nullptr, *skeys = nullptr, *perm = nullptr;
   uint32_t *offsets = nullptr;         // ncells + 1
-  uint4 *nbr = nullptr;                // neighbour lists, 8 x u16 per word (paper)
+  uint4 *nbr = nullptr;                // neighbour lists, 4 slots per word (paper)
   uint32_t *nbr_cnt = nullptr;         // neighbour counts (paper)
   uint32_t *sort_scratch = nullptr;
   uint32_t *err = nullptr;             // device error flag word
   SceneDesc *scenes = nullptr;         // device scene table
   float4 *io_pos = nullptr, *io_vel = nullptr; // input-order staging
-  // batches only (null / 1 for a single scene)
+  // batches only (null for a single scene)
   uint16_t *sid = nullptr;             // scene of each sorted slot
-  uint32_t *tile_base = nullptr;       // first gather tile of each scene (+ total)
-  uint32_t nscenes = 1;
 };
 
 // Fills dst[0, n) with `value`.
@@ -145,9 +142,8 @@ cudaError_t iota_range(uint32_t *dst, uint32_t n, cudaStream_t st);
 // Raises the dynamic shared-memory limit of the gather kernels (once per
 // process and device, before the first launch).
 cudaError_t paper_configure();
-// Tiles (CTAs) of the gather passes for n particles of one scene.
-uint32_t paper_tiles(uint32_t n);
-uint32_t paper_scene_tiles(uint32_t n_scene);
+// 16-byte list words per particle for a list capacity of maxn neighbours.
+inline uint32_t paper_list_words(uint32_t maxn) { return (maxn + 3u) / 4u; }
 cudaError_t paper_predict_hash(const float4 *X, const float4 *V, uint32_t n,
                                const PaperConsts &c, const SceneDesc *scenes,
                                const uint16_t *sid, uint32_t *keys,

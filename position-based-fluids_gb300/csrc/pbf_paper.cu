@@ -24,38 +24,31 @@
 // cells around k's cell.  Every later pass evaluates the kernels at the
 // current positions with W = 0 beyond h.
 //
-// Gather passes work on tiles of kTile consecutive sorted particles, one
-// thread each.  Sorted by cell key, a tile's particles sit in a few
-// consecutive x-rows of the grid; the 27-cell neighbourhoods of each row's
-// share lie in 9 row ranges (the share's x span widened by one cell, in the
-// rows y-1..y+1, z-1..z+1), which are contiguous slot ranges of the sorted
-// arrays: 27 ranges for a tile of at most kMaxParts = 3 rows.  Neighbour
-// lists store each neighbour as 16 bits, the range (5 bits) and the offset
-// inside it (11 bits), eight per 16-byte word:
-// group g of particle k is nbr4[g*N + k], so a warp reads its particles' next
-// eight neighbours with one coalesced load per thread, and the neighbour
-// loads that follow are independent.  A tile spanning more than
-// three rows (sparse regions) or two scenes, a range longer than 2048 slots,
-// and a particle whose set exceeds the list capacity re-derive the set from
-// the cells and the step-start positions in every pass instead (same order,
-// same arithmetic).
+// Gather passes run one thread per sorted particle.  Neighbour lists hold
+// each neighbour as its 32-bit sorted slot, four per 16-byte word: group g of
+// particle k is nbr4[g*N + k], so a warp reads its particles' next four
+// neighbours with one coalesced load per thread, and the four neighbour loads
+// that follow are independent.  A particle whose set exceeds the list
+// capacity re-derives it from the cells and the step-start positions in
+// every pass instead (same order, same arithmetic).
 //
-// The neighbour data itself is gathered through L1: measured on GB300, a
-// variant that first staged each tile's ranges into shared memory with
-// cp.async.bulk (mbarrier completion) ran 1.1-2x slower per pass than these
-// L1 gathers -- the copy latency serialises with the compute of a tile and
-// the staging buffers cap occupancy, while L1 already serves ~70% of the
-// neighbour reads.
+// Measured on GB300 (1M-particle dam break after 500 steps, per step):
+// absolute 32-bit entries run 9% faster than 16-bit entries relative to a
+// per-tile table of row ranges -- the decode and the per-tile set-up cost
+// more issue slots than the larger lists cost DRAM time (the passes run at
+// ~15-20% of DRAM bandwidth); a variant that first staged each tile's
+// neighbourhood into shared memory with cp.async.bulk ran 1.1-2x slower than
+// these L1 gathers; a persistent grid that kept neighbouring tiles on one SM
+// raised the L1 hit rate from 69% to 77% but ran 4% slower; four threads per
+// particle (neighbour entries split between them, shuffle reduction) ran
+// 1.4x slower.
 #include "pbf_device.cuh"
 
 namespace pbf {
 
 namespace {
 
-constexpr int kTile = 128;          // particles (threads) per gather CTA
-constexpr uint32_t kRelBits = 11;   // offset bits of a list entry
-constexpr uint32_t kRelMax = 1u << kRelBits;
-constexpr uint32_t kMaxParts = 3;   // x-rows a listed tile may span
+constexpr int kGather = 128;  // threads per CTA of the gather passes
 
 struct NbrCtx {
   const uint4 *__restrict__ nbr4;
@@ -66,23 +59,9 @@ struct NbrCtx {
   const float4 *__restrict__ V2;
   const SceneDesc *__restrict__ scenes;
   const uint16_t *__restrict__ sid;
-  // Batches: first tile of each scene (nscenes + 1 entries); tiles never
-  // straddle scenes.  Null for a single scene.
-  const uint32_t *__restrict__ tile_base;
-  uint32_t nscenes;
   uint32_t *err;
   uint32_t n, maxn;
   float dt, h2;
-};
-
-// Per-CTA description of the tile's neighbourhood ranges.
-struct Ranges {
-  uint32_t S[32];    // first slot of each row range (9 per part)
-  uint32_t len[32];  // slots in each row range
-  uint32_t row_a, nparts, xa[kMaxParts], xb[kMaxParts];
-  uint32_t listed;   // 1: lists encode this tile's neighbours; 0: fallback
-  uint32_t scene;
-  uint32_t k0, k1;   // first and last particle of the tile
 };
 
 __device__ __forceinline__ const SceneDesc &scene_of(const SceneDesc *scenes,
@@ -91,132 +70,40 @@ __device__ __forceinline__ const SceneDesc &scene_of(const SceneDesc *scenes,
   return scenes[sid ? sid[k] : 0];
 }
 
-__host__ __device__ __forceinline__ uint32_t gather_tiles(uint32_t n) {
-  return (n + kTile - 1) / kTile;
-}
-
-// Computes the row ranges of tile `tile` (particles [tile*kTile, +kTile)):
-// range 9*part + (dz+1)*3 + (dy+1) covers, in row (y+dy, z+dz), the cells
-// x in [xa-1, xb+1] clipped to the row, where part p is the tile's (p+1)-th
-// row and [xa, xb] the x span of its particles there.  Every pass of
-// a step computes the same result (it depends only on the sort).  Returns
-// false, uniformly, for a tile past the end.
-__device__ __forceinline__ bool ranges_setup(Ranges &w, uint32_t tile, const NbrCtx &c) {
-  // Tile -> particles.  In a batch, tiles are numbered scene by scene and
-  // start at the scene's first particle, so a scene's tiles are the same
-  // alone and in any mix.
-  uint32_t k0, kend;
-  if (c.tile_base) {
-    if (tile >= __ldg(&c.tile_base[c.nscenes])) return false;
-    uint32_t lo = 0, hi = c.nscenes - 1;  // largest s with tile_base[s] <= tile
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi + 1) >> 1;
-      if (__ldg(&c.tile_base[mid]) <= tile) lo = mid;
-      else hi = mid - 1;
-    }
-    const SceneDesc &s = c.scenes[lo];
-    k0 = s.p_begin + (tile - __ldg(&c.tile_base[lo])) * (uint32_t)kTile;
-    kend = s.p_end;
-  } else {
-    k0 = tile * (uint32_t)kTile;
-    kend = c.n;
-  }
-  if (k0 >= kend) return false;
-  const uint32_t k1 = min(k0 + (uint32_t)kTile, kend) - 1u;
-  if (threadIdx.x == 0) {
-    w.k0 = k0;
-    w.k1 = k1;
-    const uint32_t s0 = c.sid ? c.sid[k0] : 0u;
-    const uint32_t s1 = c.sid ? c.sid[k1] : 0u;
-    const SceneDesc &sc = c.scenes[s0];
-    const uint32_t nx = (uint32_t)sc.ncell[0];
-    const uint32_t a = c.skeys[k0] - sc.cell_base, b = c.skeys[k1] - sc.cell_base;
-    const uint32_t ra = a / nx, rb = b / nx;
-    w.scene = s0;
-    w.row_a = ra;
-    w.nparts = (s0 == s1 && rb >= ra && rb < ra + kMaxParts) ? (rb - ra + 1u) : 0u;
-    for (uint32_t p = 0; p < kMaxParts; ++p) {
-      w.xa[p] = p == 0 ? a % nx : 0u;
-      w.xb[p] = ra + p == rb ? b % nx : nx - 1u;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    const uint32_t t = threadIdx.x, part = t / 9u, q = t % 9u;
-    uint32_t S = 0, L = 0;
-    if (t < 9u * kMaxParts && part < w.nparts) {
-      const SceneDesc &sc = c.scenes[w.scene];
-      const uint32_t nx = (uint32_t)sc.ncell[0], ny = (uint32_t)sc.ncell[1], nz = (uint32_t)sc.ncell[2];
-      const uint32_t row = w.row_a + part;
-      const int yy = (int)(row % ny) + (int)(q % 3u) - 1;
-      const int zz = (int)(row / ny) + (int)(q / 3u) - 1;
-      if (yy >= 0 && yy < (int)ny && zz >= 0 && zz < (int)nz) {
-        const uint32_t rk = sc.cell_base + nx * ((uint32_t)yy + ny * (uint32_t)zz);
-        const uint32_t lo = rk + (w.xa[part] > 0 ? w.xa[part] - 1u : 0u);
-        const uint32_t hi = rk + min(w.xb[part] + 1u, nx - 1u);
-        S = __ldg(&c.off[lo]);
-        L = __ldg(&c.off[hi + 1]) - S;
-      }
-    }
-    w.S[t] = S;
-    w.len[t] = L;
-    // Lists can encode the tile iff it has a row decomposition and every
-    // range fits the 11-bit offset (always, short of a hundred particles per
-    // cell); otherwise the whole tile takes the fallback.
-    const bool fits = __all_sync(0xffffffffu, L <= kRelMax && (uint64_t)S + L <= c.n);
-    if (t == 0) w.listed = (w.nparts > 0 && fits) ? 1u : 0u;
-  }
-  __syncthreads();
-  return true;
-}
-
-// Slot of list entry e: S[range] + offset, clamped so that a stale entry
-// can never address past the arrays.
-__device__ __forceinline__ uint32_t entry_slot(const Ranges &w, uint32_t e, uint32_t n) {
-  return min(w.S[(e >> kRelBits) & 31u] + (e & (kRelMax - 1u)), n - 1u);
-}
-
-// For the `cnt` listed neighbours of particle k: per half group of four,
-// first load(slot) for all four (unconditionally; past-the-end entries read
-// a valid slot), then f(data, valid) for each -- so that the four gathers
-// are in flight together instead of one after another.  (Four rather than
-// eight: measured on GB300, the smaller batch keeps the lambda and delta-p
-// kernels at 40 registers, 12 CTAs per SM, and runs ~5% faster.)
+// For the `cnt` listed neighbours of particle k: per group of four, first
+// load(slot) for all four, then f(data, valid) for each.
 template <typename Load, typename F>
-__device__ __forceinline__ void for_each_listed(const NbrCtx &c, const Ranges &w, uint32_t k,
-                                                uint32_t cnt, Load &&load, F &&f) {
-  const uint32_t groups = (cnt + 7u) >> 3;
+__device__ __forceinline__ void for_each_listed(const NbrCtx &c, uint32_t k, uint32_t cnt,
+                                                Load &&load, F &&f) {
+  const uint32_t groups = (cnt + 3u) >> 2;
   for (uint32_t g = 0; g < groups; ++g) {
     const uint4 v = __ldg(&c.nbr4[(size_t)g * c.n + k]);
-    const uint32_t rem = cnt - (g << 3);
-    const uint32_t words[4] = {v.x, v.y, v.z, v.w};
+    const uint32_t rem = cnt - (g << 2);
+    const uint32_t slot[4] = {min(v.x, c.n - 1u), min(v.y, c.n - 1u), min(v.z, c.n - 1u),
+                              min(v.w, c.n - 1u)};
+    decltype(load(0u)) data[4];
 #pragma unroll
-    for (int h = 0; h < 8; h += 4) {
-      if ((uint32_t)h >= rem) break;
-      decltype(load(0u)) data[4];
+    for (int e = 0; e < 4; ++e) data[e] = load(slot[e]);
 #pragma unroll
-      for (int e = 0; e < 4; ++e)
-        data[e] = load(entry_slot(w, (words[(h + e) >> 1] >> (((h + e) & 1) * 16)) & 0xFFFFu, c.n));
-#pragma unroll
-      for (int e = 0; e < 4; ++e) f(data[e], (uint32_t)(h + e) < rem);
-    }
+    for (int e = 0; e < 4; ++e) f(data[e], (uint32_t)e < rem);
   }
 }
 
-// Accumulates one particle's list entries and writes them a group at a time.
+// Accumulates one particle's list entries and writes them four at a time.
 struct ListWriter {
-  uint64_t lo = 0, hi = 0;
+  uint32_t e[4] = {0, 0, 0, 0};
   __device__ __forceinline__ void put(uint4 *nbr4, uint32_t n, uint32_t k, uint32_t slot,
-                                      uint32_t e16) {
-    const uint32_t e = slot & 7u;
-    if (e < 4) lo |= (uint64_t)e16 << (16u * e);
-    else hi |= (uint64_t)e16 << (16u * (e - 4u));
-    if (e == 7u) flush(nbr4, n, k, slot >> 3);
+                                      uint32_t j) {
+    const uint32_t i = slot & 3u;
+    if (i == 0) e[0] = j;
+    else if (i == 1) e[1] = j;
+    else if (i == 2) e[2] = j;
+    else e[3] = j;
+    if (i == 3u) flush(nbr4, n, k, slot >> 2);
   }
   __device__ __forceinline__ void flush(uint4 *nbr4, uint32_t n, uint32_t k, uint32_t group) {
-    nbr4[(size_t)group * n + k] =
-        make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
-    lo = hi = 0;
+    nbr4[(size_t)group * n + k] = make_uint4(e[0], e[1], e[2], e[3]);
+    e[0] = e[1] = e[2] = e[3] = 0;
   }
 };
 
@@ -320,12 +207,12 @@ __device__ __forceinline__ void visit_fallback(const NbrCtx &c, uint32_t k, F &&
 
 // Calls f(load(slot), true) for every neighbour of particle k (and, in the
 // listed path, f(..., false) for the padding of the last group): from the
-// list when the tile is listed and k's set fits, otherwise re-derived.
+// list when k's set fits, otherwise re-derived.
 template <typename Load, typename F>
-__device__ __forceinline__ void visit_neighbours(const NbrCtx &c, const Ranges &w, uint32_t k,
-                                                 Load &&load, F &&f) {
+__device__ __forceinline__ void visit_neighbours(const NbrCtx &c, uint32_t k, Load &&load,
+                                                 F &&f) {
   const uint32_t cnt = c.cnt[k];
-  if (w.listed && cnt <= c.maxn) for_each_listed(c, w, k, cnt, load, f);
+  if (cnt <= c.maxn) for_each_listed(c, k, cnt, load, f);
   else visit_fallback(c, k, [&](uint32_t j) { f(load(j), true); });
 }
 
@@ -425,54 +312,43 @@ __global__ void __launch_bounds__(256)
 }
 
 // Neighbour-list build over the 27 cells, fused with the first lambda pass.
-__global__ void __launch_bounds__(kTile)
+__global__ void __launch_bounds__(kGather)
     k_nbr_lambda(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
                  uint4 *__restrict__ nbr4, uint32_t *__restrict__ nbr_cnt,
                  float4 *__restrict__ Q, float *__restrict__ R) {
-  __shared__ Ranges w;
-  if (!ranges_setup(w, blockIdx.x, nc)) return;
-  const uint32_t k = w.k0 + threadIdx.x;
-  if (k > w.k1) return;
-  const bool listed = w.listed != 0;
-  const SceneDesc &sc = nc.scenes[w.scene];
+  const uint32_t k = blockIdx.x * kGather + threadIdx.x;
+  if (k >= c.n) return;
+  const SceneDesc &sc = scene_of(nc.scenes, nc.sid, k);
   const float4 pk = P[k];
   LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
   ListWriter lw;
   uint32_t cnt = 0;
   const uint32_t key = nc.skeys[k];
-  // First range of the tile's row (part) this particle belongs to.
-  const uint32_t part = 9u * ((key - sc.cell_base) / (uint32_t)sc.ncell[0] - w.row_a);
   scan_rows_batched(k, key, sc, nc.off, [&](uint32_t j) { return __ldg(&P[j]); },
-                    [&](int q0, uint32_t j, float4 pj, bool valid) {
+                    [&](int, uint32_t j, float4 pj, bool valid) {
     const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
     if (valid && r2 > 0.0f && r2 < c.h2) {
-      // (part is meaningful for listed tiles only; the clamp keeps the
-      // shared-memory read in bounds for the others)
-      const uint32_t q = min(part + (uint32_t)q0, 31u);
-      const uint32_t rel = j - w.S[q];
-      if (listed && cnt < c.maxn) lw.put(nbr4, c.n, k, cnt, (q << kRelBits) | (rel & (kRelMax - 1u)));
+      if (cnt < c.maxn) lw.put(nbr4, c.n, k, cnt, j);
       ++cnt;
       acc.add(rx, ry, rz, r2, c);
     }
   });
-  if (listed && cnt <= c.maxn && (cnt & 7u)) lw.flush(nbr4, c.n, k, cnt >> 3);
+  if (cnt <= c.maxn && (cnt & 3u)) lw.flush(nbr4, c.n, k, cnt >> 2);
   nbr_cnt[k] = cnt;
   Q[k] = make_float4(pk.x, pk.y, pk.z, acc.lambda(c));
   R[k] = acc.rho;
 }
 
-__global__ void __launch_bounds__(kTile)
+__global__ void __launch_bounds__(kGather)
     k_lambda(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
              float4 *__restrict__ Q, float *__restrict__ R) {
-  __shared__ Ranges w;
-  if (!ranges_setup(w, blockIdx.x, nc)) return;
-  const uint32_t k = w.k0 + threadIdx.x;
-  if (k > w.k1) return;
+  const uint32_t k = blockIdx.x * kGather + threadIdx.x;
+  if (k >= c.n) return;
   const float4 pk = P[k];
   LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
   visit_neighbours(
-      nc, w, k, [&](uint32_t j) { return __ldg(&P[j]); },
+      nc, k, [&](uint32_t j) { return __ldg(&P[j]); },
       [&](float4 pj, bool valid) {
         const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
         const float r2 = rx * rx + ry * ry + rz * rz;
@@ -482,18 +358,16 @@ __global__ void __launch_bounds__(kTile)
   R[k] = acc.rho;
 }
 
-__global__ void __launch_bounds__(kTile)
+__global__ void __launch_bounds__(kGather)
     k_delta(const float4 *__restrict__ Q, NbrCtx nc, PaperConsts c,
             float4 *__restrict__ D, float4 *__restrict__ P,
             const float *__restrict__ R, float4 *__restrict__ U, int last) {
-  __shared__ Ranges w;
-  if (!ranges_setup(w, blockIdx.x, nc)) return;
-  const uint32_t k = w.k0 + threadIdx.x;
-  if (k > w.k1) return;
+  const uint32_t k = blockIdx.x * kGather + threadIdx.x;
+  if (k >= c.n) return;
   const float4 qk = Q[k];
   float sx = 0.f, sy = 0.f, sz = 0.f;
   visit_neighbours(
-      nc, w, k, [&](uint32_t j) { return __ldg(&Q[j]); },
+      nc, k, [&](uint32_t j) { return __ldg(&Q[j]); },
       [&](float4 qj, bool valid) {
         const float rx = qk.x - qj.x, ry = qk.y - qj.y, rz = qk.z - qj.z;
         const float r2 = rx * rx + ry * ry + rz * rz;
@@ -526,14 +400,12 @@ __global__ void __launch_bounds__(kTile)
 }
 
 // Vorticity omega_k; also writes (p_k, |omega_k|) into PW for the next pass.
-__global__ void __launch_bounds__(kTile)
+__global__ void __launch_bounds__(kGather)
     k_vorticity(const float4 *__restrict__ P, const float4 *__restrict__ U,
                 NbrCtx nc, PaperConsts c, float4 *__restrict__ Wo,
                 float4 *__restrict__ PW) {
-  __shared__ Ranges w;
-  if (!ranges_setup(w, blockIdx.x, nc)) return;
-  const uint32_t k = w.k0 + threadIdx.x;
-  if (k > w.k1) return;
+  const uint32_t k = blockIdx.x * kGather + threadIdx.x;
+  if (k >= c.n) return;
   const float4 pk = P[k];
   const float4 uk = U[k];
   float wx = 0.f, wy = 0.f, wz = 0.f;
@@ -541,7 +413,7 @@ __global__ void __launch_bounds__(kTile)
     float4 p, u;
   };
   visit_neighbours(
-      nc, w, k, [&](uint32_t j) { return PU{__ldg(&P[j]), __ldg(&U[j])}; },
+      nc, k, [&](uint32_t j) { return PU{__ldg(&P[j]), __ldg(&U[j])}; },
       [&](const PU &d, bool valid) {
     const float4 pj = d.p;
     const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
@@ -561,15 +433,13 @@ __global__ void __launch_bounds__(kTile)
   PW[k] = make_float4(pk.x, pk.y, pk.z, wn);
 }
 
-__global__ void __launch_bounds__(kTile)
+__global__ void __launch_bounds__(kGather)
     k_xsph_commit(const float4 *__restrict__ PW, const float4 *__restrict__ U,
                   const float4 *__restrict__ Wv, NbrCtx nc, PaperConsts c,
                   const uint32_t *__restrict__ ID2, float4 *__restrict__ X,
                   float4 *__restrict__ V, uint32_t *__restrict__ ID) {
-  __shared__ Ranges w;
-  if (!ranges_setup(w, blockIdx.x, nc)) return;
-  const uint32_t k = w.k0 + threadIdx.x;
-  if (k > w.k1) return;
+  const uint32_t k = blockIdx.x * kGather + threadIdx.x;
+  if (k >= c.n) return;
   const float4 pk = PW[k];
   const float4 uk = U[k];
   const float4 wk = Wv[k];
@@ -578,7 +448,7 @@ __global__ void __launch_bounds__(kTile)
     float4 p, u;
   };
   visit_neighbours(
-      nc, w, k, [&](uint32_t j) { return PU{__ldg(&PW[j]), __ldg(&U[j])}; },
+      nc, k, [&](uint32_t j) { return PU{__ldg(&PW[j]), __ldg(&U[j])}; },
       [&](const PU &d, bool valid) {
     const float4 pj = d.p;
     const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
@@ -670,8 +540,6 @@ NbrCtx make_ctx(const DeviceState &d, const PaperConsts &c, const uint16_t *sid)
   nc.V2 = d.V2;
   nc.scenes = d.scenes;
   nc.sid = sid;
-  nc.tile_base = d.tile_base;
-  nc.nscenes = d.nscenes;
   nc.err = d.err;
   nc.n = c.n;
   nc.maxn = c.maxn;
@@ -681,8 +549,6 @@ NbrCtx make_ctx(const DeviceState &d, const PaperConsts &c, const uint16_t *sid)
 }
 
 }  // namespace
-
-uint32_t paper_tiles(uint32_t n) { return gather_tiles(n); }
 
 cudaError_t paper_configure() { return cudaSuccess; }
 
@@ -707,33 +573,33 @@ cudaError_t paper_reorder(const uint32_t *perm, const float4 *X,
 
 cudaError_t paper_nbr_lambda(const DeviceState &d, const PaperConsts &c,
                              const uint16_t *sid, cudaStream_t st) {
-  k_nbr_lambda<<<c.tiles, kTile, 0, st>>>(d.P, make_ctx(d, c, sid), c, d.nbr, d.nbr_cnt,
+  k_nbr_lambda<<<blocks_for(c.n, kGather), kGather, 0, st>>>(d.P, make_ctx(d, c, sid), c, d.nbr, d.nbr_cnt,
                                           d.Q, d.R);
   return cudaGetLastError();
 }
 
 cudaError_t paper_lambda(const DeviceState &d, const PaperConsts &c,
                          const uint16_t *sid, cudaStream_t st) {
-  k_lambda<<<c.tiles, kTile, 0, st>>>(d.P, make_ctx(d, c, sid), c, d.Q, d.R);
+  k_lambda<<<blocks_for(c.n, kGather), kGather, 0, st>>>(d.P, make_ctx(d, c, sid), c, d.Q, d.R);
   return cudaGetLastError();
 }
 
 cudaError_t paper_delta(const DeviceState &d, const PaperConsts &c,
                         const uint16_t *sid, bool last, cudaStream_t st) {
-  k_delta<<<c.tiles, kTile, 0, st>>>(d.Q, make_ctx(d, c, sid), c, d.D, d.P, d.R, d.U,
+  k_delta<<<blocks_for(c.n, kGather), kGather, 0, st>>>(d.Q, make_ctx(d, c, sid), c, d.D, d.P, d.R, d.U,
                                      last ? 1 : 0);
   return cudaGetLastError();
 }
 
 cudaError_t paper_vorticity(const DeviceState &d, const PaperConsts &c,
                             const uint16_t *sid, cudaStream_t st) {
-  k_vorticity<<<c.tiles, kTile, 0, st>>>(d.P, d.U, make_ctx(d, c, sid), c, d.W, d.D);
+  k_vorticity<<<blocks_for(c.n, kGather), kGather, 0, st>>>(d.P, d.U, make_ctx(d, c, sid), c, d.W, d.D);
   return cudaGetLastError();
 }
 
 cudaError_t paper_xsph_commit(const DeviceState &d, const PaperConsts &c,
                               const uint16_t *sid, cudaStream_t st) {
-  k_xsph_commit<<<c.tiles, kTile, 0, st>>>(d.D, d.U, d.W, make_ctx(d, c, sid), c, d.ID2,
+  k_xsph_commit<<<blocks_for(c.n, kGather), kGather, 0, st>>>(d.D, d.U, d.W, make_ctx(d, c, sid), c, d.ID2,
                                            d.X, d.V, d.ID);
   return cudaGetLastError();
 }
@@ -776,7 +642,5 @@ cudaError_t fill_u16(uint16_t *dst, uint32_t n, uint16_t value, cudaStream_t st)
   k_fill_u16<<<blocks_for(n, 256), 256, 0, st>>>(dst, n, value);
   return cudaGetLastError();
 }
-
-uint32_t paper_scene_tiles(uint32_t n_scene) { return gather_tiles(n_scene); }
 
 }  // namespace pbf

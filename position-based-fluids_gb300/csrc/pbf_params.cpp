@@ -90,7 +90,6 @@ PaperConsts make_paper_consts(const pbf_params &p, uint32_t n) {
   c.n = n;
   // Lists are stored in groups of eight entries.
   c.maxn = p.max_neighbours < 8 ? 8u : (p.max_neighbours / 8u) * 8u;
-  c.tiles = 0;
   return c;
 }
 

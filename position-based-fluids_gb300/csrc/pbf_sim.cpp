@@ -277,7 +277,6 @@ int pbf_create(const pbf_params *params, const pbf_particle *particles,
   s->rc = make_ref_consts(*params);
   s->rc.n = n;
   s->pc = make_paper_consts(*params, n);
-  s->pc.tiles = paper_tiles(n);
   s->plan = make_sort_plan(n, bits_for(s->ncells));
   *out = s.release();
   return PBF_OK;
@@ -318,7 +317,7 @@ int pbf_init(pbf_sim *s) {
     A(&d.W, n);
     A(&d.R, n);
     A(&d.nbr_cnt, n);
-    A(&d.nbr, (size_t)(s->pc.maxn / 8u) * n);
+    A(&d.nbr, (size_t)paper_list_words(s->pc.maxn) * n);
   } else {
     A(&d.P2, n);
     A(&d.DV, n);

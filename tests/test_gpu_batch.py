@@ -9,8 +9,9 @@ K steps in a batch are BIT-IDENTICAL to
 
 whatever other scenes share the batch, and across removals and additions of
 other scenes between steps.  The scene ranges of the sorted state never mix
-(keys are scene-major) and the gather tiles start at each scene's first
-particle, so every particle runs the same instructions on the same operands.
+(keys are scene-major) and every kernel works on one particle per thread with
+neighbours from its own scene, so every particle runs the same instructions
+on the same operands.
 """
 from __future__ import annotations
 
