@@ -140,8 +140,8 @@ int launch_batch_step(pbf_batch *b) {
   PBF_TRY(paper_reorder(d.perm, d.X, d.V, d.ID, n, pc, d.X2, d.V2, d.ID2, d.P, d.D, st));
   const uint32_t iters = b->solver.solver_iterations;
   for (uint32_t it = 0; it < iters; ++it) {
-    if (it == 0) PBF_TRY(paper_nbr_lambda(d, pc, d.sid, st));
-    else PBF_TRY(paper_lambda(d, pc, d.sid, st));
+    if (it == 0) PBF_TRY(paper_nbr_build(d, pc, d.sid, st));
+    PBF_TRY(paper_lambda(d, pc, d.sid, st));
     PBF_TRY(paper_delta(d, pc, d.sid, it + 1 == iters, st));
   }
   PBF_TRY(paper_vorticity(d, pc, d.sid, st));
@@ -417,7 +417,7 @@ int pbf_batch_launches_per_step(const pbf_batch *b, uint32_t *launches) {
   if (!b || !launches) return PBF_ERR_INVALID;
   const SortPlan plan = make_sort_plan(std::max<uint32_t>(b->n_total, 1),
                                        bits_for(std::max<uint32_t>(b->cells_total, 1)));
-  *launches = 1u + 1u + plan.passes + 1u + 1u + 2u * b->solver.solver_iterations + 2u;
+  *launches = 1u + 1u + plan.passes + 1u + 1u + 1u + 2u * b->solver.solver_iterations + 2u;
   return PBF_OK;
 }
 

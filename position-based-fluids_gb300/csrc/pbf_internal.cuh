@@ -153,8 +153,9 @@ cudaError_t paper_reorder(const uint32_t *perm, const float4 *X,
                           const float4 *V, const uint32_t *ID, uint32_t n,
                           const PaperConsts &c, float4 *X2, float4 *V2,
                           uint32_t *ID2, float4 *P, float4 *D, cudaStream_t st);
-cudaError_t paper_nbr_lambda(const DeviceState &d, const PaperConsts &c,
-                             const uint16_t *sid, cudaStream_t st);
+// Neighbour lists of the step (from the predicted positions P).
+cudaError_t paper_nbr_build(const DeviceState &d, const PaperConsts &c,
+                            const uint16_t *sid, cudaStream_t st);
 cudaError_t paper_lambda(const DeviceState &d, const PaperConsts &c,
                          const uint16_t *sid, cudaStream_t st);
 cudaError_t paper_delta(const DeviceState &d, const PaperConsts &c,

@@ -89,24 +89,6 @@ __device__ __forceinline__ void for_each_listed(const NbrCtx &c, uint32_t k, uin
   }
 }
 
-// Accumulates one particle's list entries and writes them four at a time.
-struct ListWriter {
-  uint32_t e[4] = {0, 0, 0, 0};
-  __device__ __forceinline__ void put(uint4 *nbr4, uint32_t n, uint32_t k, uint32_t slot,
-                                      uint32_t j) {
-    const uint32_t i = slot & 3u;
-    if (i == 0) e[0] = j;
-    else if (i == 1) e[1] = j;
-    else if (i == 2) e[2] = j;
-    else e[3] = j;
-    if (i == 3u) flush(nbr4, n, k, slot >> 2);
-  }
-  __device__ __forceinline__ void flush(uint4 *nbr4, uint32_t n, uint32_t k, uint32_t group) {
-    nbr4[(size_t)group * n + k] = make_uint4(e[0], e[1], e[2], e[3]);
-    e[0] = e[1] = e[2] = e[3] = 0;
-  }
-};
-
 // v' = v + dt g;  d = dt v';  p = x + d  -- rounded op by op (no
 // contraction) so that every kernel that recomputes them gets the same bits.
 __device__ __forceinline__ float4 gravity_velocity(float4 v, float dt, float gy) {
@@ -311,33 +293,55 @@ __global__ void __launch_bounds__(256)
   D[k] = make_float4(d.x, d.y, d.z, 0.0f);
 }
 
-// Neighbour-list build over the 27 cells, fused with the first lambda pass.
+// Neighbour-list build over the 27 cells from the predicted positions P
+// (which equal the step-start positions the fallback recomputes).  Each
+// member's slot is stored straight into its list word; entries past the
+// count in the last word are left as they are (readers mask them).  The
+// self pair and coincident particles drop out through r^2 > 0.
 __global__ void __launch_bounds__(kGather)
-    k_nbr_lambda(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
-                 uint4 *__restrict__ nbr4, uint32_t *__restrict__ nbr_cnt,
-                 float4 *__restrict__ Q, float *__restrict__ R) {
+    k_nbr_build(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
+                uint4 *__restrict__ nbr4, uint32_t *__restrict__ nbr_cnt) {
   const uint32_t k = blockIdx.x * kGather + threadIdx.x;
   if (k >= c.n) return;
-  const SceneDesc &sc = scene_of(nc.scenes, nc.sid, k);
+  const SceneDesc &s = scene_of(nc.scenes, nc.sid, k);
   const float4 pk = P[k];
-  LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
-  ListWriter lw;
+  const int nx = s.ncell[0], ny = s.ncell[1], nz = s.ncell[2];
+  const uint32_t local = nc.skeys[k] - s.cell_base;
+  const int cx = (int)(local % (uint32_t)nx);
+  const uint32_t t = local / (uint32_t)nx;
+  const int cy = (int)(t % (uint32_t)ny);
+  const int cz = (int)(t / (uint32_t)ny);
+  const int x0 = cx > 0 ? cx - 1 : 0;
+  const int x1 = cx + 1 < nx ? cx + 1 : nx - 1;
+  uint32_t *__restrict__ out = reinterpret_cast<uint32_t *>(nbr4) + 4ull * k;
+  const size_t stride = 4ull * c.n;  // words from one list group to the next
   uint32_t cnt = 0;
-  const uint32_t key = nc.skeys[k];
-  scan_rows_batched(k, key, sc, nc.off, [&](uint32_t j) { return __ldg(&P[j]); },
-                    [&](int, uint32_t j, float4 pj, bool valid) {
-    const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
-    const float r2 = rx * rx + ry * ry + rz * rz;
-    if (valid && r2 > 0.0f && r2 < c.h2) {
-      if (cnt < c.maxn) lw.put(nbr4, c.n, k, cnt, j);
-      ++cnt;
-      acc.add(rx, ry, rz, r2, c);
+  for (int dz = -1; dz <= 1; ++dz) {
+    const int z = cz + dz;
+    if (z < 0 || z >= nz) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = cy + dy;
+      if (y < 0 || y >= ny) continue;
+      const uint32_t row = s.cell_base + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+      const uint32_t a = __ldg(&nc.off[row + x0]);
+      const uint32_t b = __ldg(&nc.off[row + x1 + 1]);
+      for (uint32_t j = a; j < b; j += 4) {
+        float4 d[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) d[e] = __ldg(&P[min(j + e, b - 1u)]);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
+          const float r2 = rx * rx + ry * ry + rz * rz;
+          if (j + e < b && r2 > 0.0f && r2 < c.h2) {
+            if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j + e;
+            ++cnt;
+          }
+        }
+      }
     }
-  });
-  if (cnt <= c.maxn && (cnt & 3u)) lw.flush(nbr4, c.n, k, cnt >> 2);
+  }
   nbr_cnt[k] = cnt;
-  Q[k] = make_float4(pk.x, pk.y, pk.z, acc.lambda(c));
-  R[k] = acc.rho;
 }
 
 __global__ void __launch_bounds__(kGather)
@@ -571,10 +575,10 @@ cudaError_t paper_reorder(const uint32_t *perm, const float4 *X,
   return cudaGetLastError();
 }
 
-cudaError_t paper_nbr_lambda(const DeviceState &d, const PaperConsts &c,
-                             const uint16_t *sid, cudaStream_t st) {
-  k_nbr_lambda<<<blocks_for(c.n, kGather), kGather, 0, st>>>(d.P, make_ctx(d, c, sid), c, d.nbr, d.nbr_cnt,
-                                          d.Q, d.R);
+cudaError_t paper_nbr_build(const DeviceState &d, const PaperConsts &c,
+                            const uint16_t *sid, cudaStream_t st) {
+  k_nbr_build<<<blocks_for(c.n, kGather), kGather, 0, st>>>(d.P, make_ctx(d, c, sid), c, d.nbr,
+                                                           d.nbr_cnt);
   return cudaGetLastError();
 }
 

@@ -146,12 +146,11 @@ int launch_step(pbf_sim *s) {
     const uint32_t iters = s->prm.solver_iterations;
     for (uint32_t it = 0; it < iters; ++it) {
       if (it == 0) {
-        PBF_TRY(paper_nbr_lambda(d, s->pc, nullptr, st));
-        PBF_TRY_STATUS(mark(s, 1, "nbr_lambda", 1, &ev));
-      } else {
-        PBF_TRY(paper_lambda(d, s->pc, nullptr, st));
-        PBF_TRY_STATUS(mark(s, 1, "lambda", 1, &ev));
+        PBF_TRY(paper_nbr_build(d, s->pc, nullptr, st));
+        PBF_TRY_STATUS(mark(s, 1, "nbr_build", 1, &ev));
       }
+      PBF_TRY(paper_lambda(d, s->pc, nullptr, st));
+      PBF_TRY_STATUS(mark(s, 1, "lambda", 1, &ev));
       PBF_TRY(paper_delta(d, s->pc, nullptr, it + 1 == iters, st));
       PBF_TRY_STATUS(mark(s, 2, "delta", 1, &ev));
     }
@@ -508,7 +507,7 @@ int pbf_launches_per_step(const pbf_sim *s, uint32_t *launches) {
   const uint32_t it = s->prm.solver_iterations;
   const uint32_t sort = 1u /*scan*/ + s->plan.passes + 1u /*offsets*/;
   if (s->paper)
-    *launches = 1u /*predict+hash*/ + sort + 1u /*reorder*/ + 2u * it + 2u;
+    *launches = 1u /*predict+hash*/ + sort + 1u /*reorder*/ + 1u /*lists*/ + 2u * it + 2u;
   else
     *launches = 1u + sort + 2u * it + 2u;
   return PBF_OK;
