@@ -232,6 +232,8 @@ def run_ours(args) -> int:
     sim = pbf.Simulation(sc.params, sc.particles)
     sim.init()
     sim.initCells()
+    if args.load_state:
+        sim.load_state(args.load_state)
     ext = torch.cuda.ExternalStream(sim.stream())
     launches = sim.launches_per_step()
 
@@ -254,6 +256,8 @@ def run_ours(args) -> int:
     t_dev = reduce_max(dist, t_dev, device="cuda")
     value = world * n * ITERATIONS * args.steps / t_dev
     clock_summary = clocks.summary()
+    if args.save_state and rank == 0:
+        sim.save_state(args.save_state)
 
     # ---- end to end through the C-ABI with host buffers ------------------
     nbytes = n * 16
@@ -329,7 +333,7 @@ def run_ours(args) -> int:
                        "equations": "paper (relaxation 600, s_corr, XSPH, vorticity)",
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set larger than L2; no flush between steps",
-                       "graph": True},
+                       "graph": True, "start_state": args.load_state or "initial block"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
                     "d2h_bytes_per_step": 2 * nbytes, "steps": e2e_steps, "finite": finite},
             "gpu_launches": launches * args.steps,
@@ -593,6 +597,10 @@ def main() -> int:
     ap.add_argument("--plain-sample", type=int, default=30,
                     help="timed steps per scene of the one-by-one plain comparison")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-by-one plain comparison")
+    ap.add_argument("--save-state", default=None,
+                    help="single scene: write the state after the warm-up and timed steps (.npz)")
+    ap.add_argument("--load-state", default=None,
+                    help="single scene: start from a state written by --save-state")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

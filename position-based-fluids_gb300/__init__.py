@@ -339,6 +339,18 @@ class Simulation:
         vel = np.ascontiguousarray(vel4, np.float32).reshape(self.n, 4)
         _check(lib().pbf_set_state(self._h, _ptr(pos), _ptr(vel)), "pbf_set_state")
 
+    def save_state(self, path):
+        """Checkpoint: the state in the dumpData layout, as an .npz file."""
+        pos, vel = self.dumpData()
+        np.savez(path, pos=pos, vel=vel, n=self.n)
+
+    def load_state(self, path):
+        """Resumes from a checkpoint written by save_state."""
+        d = np.load(path)
+        if int(d["n"]) != self.n:
+            raise PbfError(ERR_INVALID, "load_state: particle count differs")
+        self.set_state(d["pos"], d["vel"])
+
     def set_state_async(self, pos_ptr: int, vel_ptr: int):
         _check(lib().pbf_set_state_async(self._h, pos_ptr, vel_ptr), "pbf_set_state_async")
 
