@@ -234,6 +234,7 @@ def run_ours(args) -> int:
     sim.initCells()
     if args.load_state:
         sim.load_state(args.load_state)
+    tuning = None if args.no_tune else sim.autotune(3).as_dict()
     ext = torch.cuda.ExternalStream(sim.stream())
     launches = sim.launches_per_step()
 
@@ -333,7 +334,8 @@ def run_ours(args) -> int:
                        "equations": "paper (relaxation 600, s_corr, XSPH, vorticity)",
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set larger than L2; no flush between steps",
-                       "graph": True, "start_state": args.load_state or "initial block"},
+                       "graph": True, "start_state": args.load_state or "initial block",
+                       "tuning": tuning},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
                     "d2h_bytes_per_step": 2 * nbytes, "steps": e2e_steps, "finite": finite},
             "gpu_launches": launches * args.steps,
@@ -403,6 +405,7 @@ def run_batch(args) -> int:
     w0 = time.perf_counter()
     b = pbf.Batch(solver, len(scenes), n_tot, cells_tot)
     ids = [b.add_scene(s.params, s.particles) for s in scenes]
+    tuning = None if args.no_tune else b.autotune(3).as_dict()
     ext = torch.cuda.ExternalStream(b.stream())
     launches = b.launches_per_step()
     b.step(args.warmup)
@@ -454,7 +457,7 @@ def run_batch(args) -> int:
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "batch_256_scenes", "scenes": len(scenes), "particles": n_tot,
                        "cells": cells_tot, "sizes": "log-uniform 4096..262144, seed 0x5EED",
-                       "solver_iterations": ITERATIONS, "graph": True,
+                       "solver_iterations": ITERATIONS, "graph": True, "tuning": tuning,
                        "equations": "paper (relaxation 600, s_corr, XSPH, vorticity)",
                        "l2": "working set larger than L2; no flush between steps"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n_tot / (steps + args.warmup),
@@ -597,6 +600,7 @@ def main() -> int:
     ap.add_argument("--plain-sample", type=int, default=30,
                     help="timed steps per scene of the one-by-one plain comparison")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-by-one plain comparison")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--save-state", default=None,
                     help="single scene: write the state after the warm-up and timed steps (.npz)")
     ap.add_argument("--load-state", default=None,

@@ -204,6 +204,29 @@ int pbf_kernel_times(pbf_sim *sim, uint32_t cap, char *names, float *total_ms,
 int pbf_set_graph(pbf_sim *sim, int enable);
 /* Number of this library's kernel launches one step issues. */
 int pbf_launches_per_step(const pbf_sim *sim, uint32_t *launches);
+
+/* Launch shape of the paper-mode gather passes, per pass: index 0 the
+ * neighbour-list build, 1 the list build fused with the first lambda, 2
+ * lambda, 3 delta-p, 4 vorticity, 5 XSPH + commit.  threads = 64, 128 or
+ * 256 per CTA; batch = 4 or 8 neighbour loads in flight per thread (ignored
+ * for 0 and 1); fuse_first = 1 runs 1 instead of 0 + 2 for the first solver
+ * iteration.  No shape changes a result bit.  trial_ms is the tuner's best
+ * time per launch of each pass (0 when untuned). */
+typedef struct pbf_tuning {
+  uint32_t threads[6];
+  uint32_t batch[6];
+  uint32_t fuse_first;
+  float trial_ms[6];
+} pbf_tuning;
+/* Times every shape over `trial_steps` steps (1..32) of this simulation
+ * from its current state, keeps the fastest per pass and restores the state
+ * (PAPER mode; a no-op returning the defaults in REF_COMPAT mode).  Later
+ * steps are bitwise the ones an untuned simulation takes.  `out` may be
+ * NULL.  No reference counterpart. */
+int pbf_autotune(pbf_sim *sim, uint32_t trial_steps, pbf_tuning *out);
+int pbf_get_tuning(const pbf_sim *sim, pbf_tuning *out);
+/* PBF_ERR_INVALID for a shape outside the values above. */
+int pbf_set_tuning(pbf_sim *sim, const pbf_tuning *tuning);
 /* Density of every particle from the last lambda pass of the last step
  * (input order). */
 int pbf_get_density(pbf_sim *sim, float *density);
@@ -252,6 +275,10 @@ int pbf_batch_info(const pbf_batch *b, uint32_t *scenes, uint32_t *particles,
                    uint32_t *cells);
 int pbf_batch_get_stream(const pbf_batch *b, void **stream);
 int pbf_batch_launches_per_step(const pbf_batch *b, uint32_t *launches);
+/* pbf_autotune for a batch, over the scenes it holds. */
+int pbf_batch_autotune(pbf_batch *b, uint32_t trial_steps, pbf_tuning *out);
+int pbf_batch_get_tuning(const pbf_batch *b, pbf_tuning *out);
+int pbf_batch_set_tuning(pbf_batch *b, const pbf_tuning *tuning);
 int pbf_batch_destroy(pbf_batch *b);
 
 /* ------------------------------------------------------- served scenes */

@@ -99,6 +99,19 @@ PARTICLE_DTYPE = np.dtype([("m", np.float32), ("x", np.float32, 3), ("v", np.flo
 assert PARTICLE_DTYPE.itemsize == C.sizeof(Particle)
 
 
+class Tuning(C.Structure):
+    """pbf_tuning: launch shape of the gather passes (list build, fused list
+    build + first lambda, lambda, delta-p, vorticity, XSPH)."""
+
+    PASSES = ("nbr_build", "nbr_lambda", "lambda", "delta", "vorticity", "xsph_commit")
+    _fields_ = [("threads", C.c_uint32 * 6), ("batch", C.c_uint32 * 6), ("fuse_first", C.c_uint32),
+                ("trial_ms", C.c_float * 6)]
+
+    def as_dict(self) -> dict:
+        return {"threads": dict(zip(self.PASSES, self.threads)), "batch": dict(zip(self.PASSES, self.batch)),
+                "fuse_first": int(self.fuse_first), "trial_ms": dict(zip(self.PASSES, self.trial_ms))}
+
+
 class ServerStats(C.Structure):
     """pbf_server_stats."""
 
@@ -169,6 +182,12 @@ def lib():
             "pbf_get_density": ([vp, vp], i32),
             "pbf_get_cells": ([vp, vp, vp, vp], i32),
             "pbf_destroy": ([vp], i32),
+            "pbf_autotune": ([vp, u32, C.POINTER(Tuning)], i32),
+            "pbf_get_tuning": ([vp, C.POINTER(Tuning)], i32),
+            "pbf_set_tuning": ([vp, C.POINTER(Tuning)], i32),
+            "pbf_batch_autotune": ([vp, u32, C.POINTER(Tuning)], i32),
+            "pbf_batch_get_tuning": ([vp, C.POINTER(Tuning)], i32),
+            "pbf_batch_set_tuning": ([vp, C.POINTER(Tuning)], i32),
             "pbf_op_cell_hash": ([pp, vp, u32, vp, vp], i32),
             "pbf_op_sort_scratch_bytes": ([u32, u32], C.c_size_t),
             "pbf_op_sort_pairs": ([vp, vp, u32, u32, vp, vp, vp, C.c_size_t, vp], i32),
@@ -422,6 +441,21 @@ class Simulation:
     def set_graph(self, enable: bool):
         _check(lib().pbf_set_graph(self._h, int(enable)), "pbf_set_graph")
 
+    def autotune(self, trial_steps: int = 3) -> Tuning:
+        """Picks the fastest launch shape of each gather pass on this scene
+        (the state is restored; results are unchanged)."""
+        t = Tuning()
+        _check(lib().pbf_autotune(self._h, trial_steps, C.byref(t)), "pbf_autotune")
+        return t
+
+    def tuning(self) -> Tuning:
+        t = Tuning()
+        _check(lib().pbf_get_tuning(self._h, C.byref(t)), "pbf_get_tuning")
+        return t
+
+    def set_tuning(self, t: Tuning):
+        _check(lib().pbf_set_tuning(self._h, C.byref(t)), "pbf_set_tuning")
+
     def launches_per_step(self) -> int:
         n = C.c_uint32()
         _check(lib().pbf_launches_per_step(self._h, C.byref(n)), "pbf_launches_per_step")
@@ -493,6 +527,19 @@ class Batch:
         n = C.c_uint32()
         _check(lib().pbf_batch_launches_per_step(self._h, C.byref(n)), "pbf_batch_launches_per_step")
         return n.value
+
+    def autotune(self, trial_steps: int = 3) -> Tuning:
+        t = Tuning()
+        _check(lib().pbf_batch_autotune(self._h, trial_steps, C.byref(t)), "pbf_batch_autotune")
+        return t
+
+    def tuning(self) -> Tuning:
+        t = Tuning()
+        _check(lib().pbf_batch_get_tuning(self._h, C.byref(t)), "pbf_batch_get_tuning")
+        return t
+
+    def set_tuning(self, t: Tuning):
+        _check(lib().pbf_batch_set_tuning(self._h, C.byref(t)), "pbf_batch_set_tuning")
 
     def close(self):
         if getattr(self, "_h", None):

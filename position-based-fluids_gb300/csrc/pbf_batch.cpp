@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "pbf_host.hpp"
+#include "pbf_tune.hpp"
 
 using namespace pbf;
 
@@ -140,8 +141,12 @@ int launch_batch_step(pbf_batch *b) {
   PBF_TRY(paper_reorder(d.perm, d.X, d.V, d.ID, n, pc, d.X2, d.V2, d.ID2, d.P, d.D, st));
   const uint32_t iters = b->solver.solver_iterations;
   for (uint32_t it = 0; it < iters; ++it) {
-    if (it == 0) PBF_TRY(paper_nbr_build(d, pc, d.sid, st));
-    PBF_TRY(paper_lambda(d, pc, d.sid, st));
+    if (it == 0 && d.tune.fuse_first) {
+      PBF_TRY(paper_nbr_lambda(d, pc, d.sid, st));
+    } else {
+      if (it == 0) PBF_TRY(paper_nbr_build(d, pc, d.sid, st));
+      PBF_TRY(paper_lambda(d, pc, d.sid, st));
+    }
     PBF_TRY(paper_delta(d, pc, d.sid, it + 1 == iters, st));
   }
   PBF_TRY(paper_vorticity(d, pc, d.sid, st));
@@ -417,7 +422,37 @@ int pbf_batch_launches_per_step(const pbf_batch *b, uint32_t *launches) {
   if (!b || !launches) return PBF_ERR_INVALID;
   const SortPlan plan = make_sort_plan(std::max<uint32_t>(b->n_total, 1),
                                        bits_for(std::max<uint32_t>(b->cells_total, 1)));
-  *launches = 1u + 1u + plan.passes + 1u + 1u + 1u + 2u * b->solver.solver_iterations + 2u;
+  *launches = 1u + 1u + plan.passes + 1u + 1u + paper_first_launches(b->d) +
+              2u * b->solver.solver_iterations - 1u + 2u;
+  return PBF_OK;
+}
+
+int pbf_batch_autotune(pbf_batch *b, uint32_t trial_steps, pbf_tuning *out) {
+  if (!b || trial_steps < 1 || trial_steps > 32) return PBF_ERR_INVALID;
+  if (b->dirty) PBF_TRY_STATUS(apply_layout(b));
+  double ms[kGatherKinds] = {0, 0, 0, 0, 0, 0};
+  if (b->n_total > 0) {
+    PBF_TRY_STATUS(paper_autotune(b->d, b->n_total, b->stream, trial_steps,
+                                  [&]() { return launch_batch_step(b); }, ms));
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    PBF_TRY_STATUS(pbf_batch_sync(b));
+  }
+  if (out) to_pbf_tuning(b->d.tune, ms, out);
+  return PBF_OK;
+}
+
+int pbf_batch_get_tuning(const pbf_batch *b, pbf_tuning *out) {
+  if (!b || !out) return PBF_ERR_INVALID;
+  to_pbf_tuning(b->d.tune, nullptr, out);
+  return PBF_OK;
+}
+
+int pbf_batch_set_tuning(pbf_batch *b, const pbf_tuning *t) {
+  if (!b || !t) return PBF_ERR_INVALID;
+  PBF_TRY_STATUS(to_gather_tuning(*t, &b->d.tune));
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
   return PBF_OK;
 }
 

@@ -39,4 +39,9 @@ int batch_check_scene(const pbf_batch *b, const pbf_params &scene, uint32_t n,
 void batch_capacity(const pbf_batch *b, uint32_t *scenes, uint32_t *particles,
                     uint32_t *cells);
 
+// pbf_tuning <-> GatherTuning.  to_gather_tuning returns PBF_ERR_INVALID for
+// a shape outside 64/128/256 threads and 4/8 loads in flight.
+void to_pbf_tuning(const GatherTuning &g, const double trial_ms[kGatherKinds], pbf_tuning *out);
+int to_gather_tuning(const pbf_tuning &t, GatherTuning *out);
+
 }  // namespace pbf

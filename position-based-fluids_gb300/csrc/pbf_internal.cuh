@@ -105,6 +105,76 @@ cudaError_t cell_hash(const float4 *pred, uint32_t n, const SceneDesc &scene,
 // Number of kernel launches of one sort (histogram not included).
 uint32_t sort_pass_launches(const SortPlan &plan);
 
+// ------------------------------------------------- gather-pass launch shape --
+// The gather passes of the paper equations, as tuned separately.
+enum GatherKind : int {
+  kKindNbr = 0,     // neighbour-list build
+  kKindNbrLambda,   // list build fused with the first lambda
+  kKindLambda,
+  kKindDelta,
+  kKindVorticity,
+  kKindXsph,
+  kGatherKinds
+};
+
+// Launch shape of each gather pass.  No choice changes a result bit: every
+// variant computes each particle in one thread with the same operations in
+// the same order.
+struct GatherTuning {
+  uint8_t block[kGatherKinds] = {1, 1, 1, 1, 1, 1};  // threads per CTA: 64 << code
+  uint8_t batch[kGatherKinds] = {0, 0, 0, 0, 0, 0};  // neighbour loads in flight: 4 << code
+  uint8_t fuse_first = 0;  // 1: one kernel builds the lists and computes the first lambda
+};
+constexpr int kBlockCodes = 3;  // 64, 128, 256
+constexpr int kBatchCodes = 2;  // 4, 8
+
+// Optional per-kind timing of gather launches (used by the tuner): an event
+// pair around each launch, summed per kind by collect().
+struct GatherTimer {
+  static constexpr int kMax = 512;
+  cudaEvent_t ev[2 * kMax] = {};
+  int kind[kMax] = {};
+  int used = 0;
+  bool ready = false;
+  cudaError_t init() {
+    for (int i = 0; i < 2 * kMax; ++i) {
+      const cudaError_t e = cudaEventCreate(&ev[i]);
+      if (e != cudaSuccess) return e;
+    }
+    ready = true;
+    return cudaSuccess;
+  }
+  void destroy() {
+    for (int i = 0; i < 2 * kMax; ++i)
+      if (ev[i]) cudaEventDestroy(ev[i]);
+    ready = false;
+  }
+  // Returns the slot to close with end(), or -1 when the pool is full.
+  int begin(int k, cudaStream_t st) {
+    if (!ready || used >= kMax) return -1;
+    kind[used] = k;
+    cudaEventRecord(ev[2 * used], st);
+    return used++;
+  }
+  void end(int slot, cudaStream_t st) {
+    if (slot >= 0) cudaEventRecord(ev[2 * slot + 1], st);
+  }
+  cudaError_t collect(double ms[kGatherKinds], uint32_t count[kGatherKinds]) {
+    for (int k = 0; k < kGatherKinds; ++k) ms[k] = 0.0, count[k] = 0;
+    for (int i = 0; i < used; ++i) {
+      cudaError_t e = cudaEventSynchronize(ev[2 * i + 1]);
+      if (e != cudaSuccess) return e;
+      float t = 0.f;
+      e = cudaEventElapsedTime(&t, ev[2 * i], ev[2 * i + 1]);
+      if (e != cudaSuccess) return e;
+      ms[kind[i]] += t;
+      count[kind[i]] += 1;
+    }
+    used = 0;
+    return cudaSuccess;
+  }
+};
+
 // --------------------------------------------------------- device buffers --
 // Everything one plain (single-scene) simulation keeps on the device.
 struct DeviceState {
@@ -131,6 +201,9 @@ struct DeviceState {
   float4 *io_pos = nullptr, *io_vel = nullptr; // input-order staging
   // batches only (null for a single scene)
   uint16_t *sid = nullptr;             // scene of each sorted slot
+  // host-side launch shape of the gather passes, and the tuner's timer
+  GatherTuning tune;
+  GatherTimer *timer = nullptr;
 };
 
 // Fills dst[0, n) with `value`.
@@ -156,6 +229,14 @@ cudaError_t paper_reorder(const uint32_t *perm, const float4 *X,
 // Neighbour lists of the step (from the predicted positions P).
 cudaError_t paper_nbr_build(const DeviceState &d, const PaperConsts &c,
                             const uint16_t *sid, cudaStream_t st);
+// The same lists and, in the same kernel, the first lambda pass.
+cudaError_t paper_nbr_lambda(const DeviceState &d, const PaperConsts &c,
+                             const uint16_t *sid, cudaStream_t st);
+// Launches of the first solver iteration's list build and lambda pass under
+// the current tuning (1 fused or 2).
+inline uint32_t paper_first_launches(const DeviceState &d) {
+  return d.tune.fuse_first ? 1u : 2u;
+}
 cudaError_t paper_lambda(const DeviceState &d, const PaperConsts &c,
                          const uint16_t *sid, cudaStream_t st);
 cudaError_t paper_delta(const DeviceState &d, const PaperConsts &c,

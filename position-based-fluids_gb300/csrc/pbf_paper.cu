@@ -48,7 +48,6 @@ namespace pbf {
 
 namespace {
 
-constexpr int kGather = 128;  // threads per CTA of the gather passes
 
 struct NbrCtx {
   const uint4 *__restrict__ nbr4;
@@ -70,22 +69,33 @@ __device__ __forceinline__ const SceneDesc &scene_of(const SceneDesc *scenes,
   return scenes[sid ? sid[k] : 0];
 }
 
-// For the `cnt` listed neighbours of particle k: per group of four, first
-// load(slot) for all four, then f(data, valid) for each.
-template <typename Load, typename F>
+// For the `cnt` listed neighbours of particle k, kBatch (4 or 8) at a time:
+// the batch's list words, then load(slot) for every entry of the batch, then
+// f(data, valid) for each in list order -- the loads of a batch are in
+// flight together.  Slots are clamped to the arrays (entries past the count
+// in the last word are whatever an earlier step left there).
+template <int kBatch, typename Load, typename F>
 __device__ __forceinline__ void for_each_listed(const NbrCtx &c, uint32_t k, uint32_t cnt,
                                                 Load &&load, F &&f) {
-  const uint32_t groups = (cnt + 3u) >> 2;
-  for (uint32_t g = 0; g < groups; ++g) {
-    const uint4 v = __ldg(&c.nbr4[(size_t)g * c.n + k]);
-    const uint32_t rem = cnt - (g << 2);
-    const uint32_t slot[4] = {min(v.x, c.n - 1u), min(v.y, c.n - 1u), min(v.z, c.n - 1u),
-                              min(v.w, c.n - 1u)};
-    decltype(load(0u)) data[4];
+  static_assert(kBatch % 4 == 0, "whole list words per batch");
+  constexpr int kWords = kBatch / 4;
+  for (uint32_t e0 = 0; e0 < cnt; e0 += kBatch) {
+    uint32_t slot[kBatch];
 #pragma unroll
-    for (int e = 0; e < 4; ++e) data[e] = load(slot[e]);
+    for (int w = 0; w < kWords; ++w) {
+      const uint32_t g = (e0 >> 2) + (uint32_t)w;
+      const uint4 v = (w == 0 || 4u * g < cnt) ? __ldg(&c.nbr4[(size_t)g * c.n + k])
+                                                : make_uint4(0u, 0u, 0u, 0u);
+      slot[4 * w + 0] = min(v.x, c.n - 1u);
+      slot[4 * w + 1] = min(v.y, c.n - 1u);
+      slot[4 * w + 2] = min(v.z, c.n - 1u);
+      slot[4 * w + 3] = min(v.w, c.n - 1u);
+    }
+    decltype(load(0u)) data[kBatch];
 #pragma unroll
-    for (int e = 0; e < 4; ++e) f(data[e], (uint32_t)e < rem);
+    for (int e = 0; e < kBatch; ++e) data[e] = load(slot[e]);
+#pragma unroll
+    for (int e = 0; e < kBatch; ++e) f(data[e], e0 + (uint32_t)e < cnt);
   }
 }
 
@@ -136,44 +146,6 @@ __device__ __forceinline__ void scan_rows(uint32_t k, uint32_t key, const SceneD
   }
 }
 
-// scan_rows with the candidates of a row taken four at a time: the four
-// loads are issued before any is used.  f(q, j, data, valid).
-template <typename Load, typename F>
-__device__ __forceinline__ void scan_rows_batched(uint32_t k, uint32_t key, const SceneDesc &s,
-                                                  const uint32_t *__restrict__ off, Load &&load,
-                                                  F &&f) {
-  const int nx = s.ncell[0], ny = s.ncell[1], nz = s.ncell[2];
-  const uint32_t local = key - s.cell_base;
-  const int cx = (int)(local % (uint32_t)nx);
-  const uint32_t t = local / (uint32_t)nx;
-  const int cy = (int)(t % (uint32_t)ny);
-  const int cz = (int)(t / (uint32_t)ny);
-  const int x0 = cx > 0 ? cx - 1 : 0;
-  const int x1 = cx + 1 < nx ? cx + 1 : nx - 1;
-  for (int dz = -1; dz <= 1; ++dz) {
-    const int z = cz + dz;
-    if (z < 0 || z >= nz) continue;
-    for (int dy = -1; dy <= 1; ++dy) {
-      const int y = cy + dy;
-      if (y < 0 || y >= ny) continue;
-      const int q = (dz + 1) * 3 + (dy + 1);
-      const uint32_t row = s.cell_base + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
-      const uint32_t a = __ldg(&off[row + x0]);
-      const uint32_t b = __ldg(&off[row + x1 + 1]);
-      for (uint32_t j = a; j < b; j += 4) {
-        decltype(load(0u)) data[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) data[e] = load(min(j + e, b - 1u));
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const uint32_t je = j + e;
-          f(q, je, data[e], je < b && je != k);
-        }
-      }
-    }
-  }
-}
-
 // Re-derives N_k from the cells and the step-start positions (global loads).
 template <typename F>
 __device__ __forceinline__ void visit_fallback(const NbrCtx &c, uint32_t k, F &&f) {
@@ -190,11 +162,11 @@ __device__ __forceinline__ void visit_fallback(const NbrCtx &c, uint32_t k, F &&
 // Calls f(load(slot), true) for every neighbour of particle k (and, in the
 // listed path, f(..., false) for the padding of the last group): from the
 // list when k's set fits, otherwise re-derived.
-template <typename Load, typename F>
+template <int kBatch, typename Load, typename F>
 __device__ __forceinline__ void visit_neighbours(const NbrCtx &c, uint32_t k, Load &&load,
                                                  F &&f) {
   const uint32_t cnt = c.cnt[k];
-  if (cnt <= c.maxn) for_each_listed(c, k, cnt, load, f);
+  if (cnt <= c.maxn) for_each_listed<kBatch>(c, k, cnt, load, f);
   else visit_fallback(c, k, [&](uint32_t j) { f(load(j), true); });
 }
 
@@ -298,10 +270,11 @@ __global__ void __launch_bounds__(256)
 // member's slot is stored straight into its list word; entries past the
 // count in the last word are left as they are (readers mask them).  The
 // self pair and coincident particles drop out through r^2 > 0.
-__global__ void __launch_bounds__(kGather)
+template <int kBlock>
+__global__ void __launch_bounds__(kBlock)
     k_nbr_build(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
                 uint4 *__restrict__ nbr4, uint32_t *__restrict__ nbr_cnt) {
-  const uint32_t k = blockIdx.x * kGather + threadIdx.x;
+  const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
   if (k >= c.n) return;
   const SceneDesc &s = scene_of(nc.scenes, nc.sid, k);
   const float4 pk = P[k];
@@ -344,14 +317,72 @@ __global__ void __launch_bounds__(kGather)
   nbr_cnt[k] = cnt;
 }
 
-__global__ void __launch_bounds__(kGather)
+// k_nbr_build fused with the first lambda pass: the same lists, and lambda
+// summed over the members in the order the lists store them -- the bits
+// k_lambda computes from the lists.  (In one kernel a warp executes the
+// lambda arithmetic whenever any of its lanes has a member, so which form is
+// faster depends on the scene; the tuner picks.)
+template <int kBlock>
+__global__ void __launch_bounds__(kBlock)
+    k_nbr_lambda(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
+                 uint4 *__restrict__ nbr4, uint32_t *__restrict__ nbr_cnt,
+                 float4 *__restrict__ Q, float *__restrict__ R) {
+  const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
+  if (k >= c.n) return;
+  const SceneDesc &s = scene_of(nc.scenes, nc.sid, k);
+  const float4 pk = P[k];
+  const int nx = s.ncell[0], ny = s.ncell[1], nz = s.ncell[2];
+  const uint32_t local = nc.skeys[k] - s.cell_base;
+  const int cx = (int)(local % (uint32_t)nx);
+  const uint32_t t = local / (uint32_t)nx;
+  const int cy = (int)(t % (uint32_t)ny);
+  const int cz = (int)(t / (uint32_t)ny);
+  const int x0 = cx > 0 ? cx - 1 : 0;
+  const int x1 = cx + 1 < nx ? cx + 1 : nx - 1;
+  uint32_t *__restrict__ out = reinterpret_cast<uint32_t *>(nbr4) + 4ull * k;
+  const size_t stride = 4ull * c.n;  // words from one list group to the next
+  uint32_t cnt = 0;
+  LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
+  for (int dz = -1; dz <= 1; ++dz) {
+    const int z = cz + dz;
+    if (z < 0 || z >= nz) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = cy + dy;
+      if (y < 0 || y >= ny) continue;
+      const uint32_t row = s.cell_base + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+      const uint32_t a = __ldg(&nc.off[row + x0]);
+      const uint32_t b = __ldg(&nc.off[row + x1 + 1]);
+      for (uint32_t j = a; j < b; j += 4) {
+        float4 d[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) d[e] = __ldg(&P[min(j + e, b - 1u)]);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
+          const float r2 = rx * rx + ry * ry + rz * rz;
+          if (j + e < b && r2 > 0.0f && r2 < c.h2) {
+            if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j + e;
+            ++cnt;
+            acc.add(rx, ry, rz, r2, c);
+          }
+        }
+      }
+    }
+  }
+  nbr_cnt[k] = cnt;
+  Q[k] = make_float4(pk.x, pk.y, pk.z, acc.lambda(c));
+  R[k] = acc.rho;
+}
+
+template <int kBlock, int kBatch>
+__global__ void __launch_bounds__(kBlock)
     k_lambda(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
              float4 *__restrict__ Q, float *__restrict__ R) {
-  const uint32_t k = blockIdx.x * kGather + threadIdx.x;
+  const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
   if (k >= c.n) return;
   const float4 pk = P[k];
   LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
-  visit_neighbours(
+  visit_neighbours<kBatch>(
       nc, k, [&](uint32_t j) { return __ldg(&P[j]); },
       [&](float4 pj, bool valid) {
         const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
@@ -362,15 +393,16 @@ __global__ void __launch_bounds__(kGather)
   R[k] = acc.rho;
 }
 
-__global__ void __launch_bounds__(kGather)
+template <int kBlock, int kBatch>
+__global__ void __launch_bounds__(kBlock)
     k_delta(const float4 *__restrict__ Q, NbrCtx nc, PaperConsts c,
             float4 *__restrict__ D, float4 *__restrict__ P,
             const float *__restrict__ R, float4 *__restrict__ U, int last) {
-  const uint32_t k = blockIdx.x * kGather + threadIdx.x;
+  const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
   if (k >= c.n) return;
   const float4 qk = Q[k];
   float sx = 0.f, sy = 0.f, sz = 0.f;
-  visit_neighbours(
+  visit_neighbours<kBatch>(
       nc, k, [&](uint32_t j) { return __ldg(&Q[j]); },
       [&](float4 qj, bool valid) {
         const float rx = qk.x - qj.x, ry = qk.y - qj.y, rz = qk.z - qj.z;
@@ -404,11 +436,12 @@ __global__ void __launch_bounds__(kGather)
 }
 
 // Vorticity omega_k; also writes (p_k, |omega_k|) into PW for the next pass.
-__global__ void __launch_bounds__(kGather)
+template <int kBlock, int kBatch>
+__global__ void __launch_bounds__(kBlock)
     k_vorticity(const float4 *__restrict__ P, const float4 *__restrict__ U,
                 NbrCtx nc, PaperConsts c, float4 *__restrict__ Wo,
                 float4 *__restrict__ PW) {
-  const uint32_t k = blockIdx.x * kGather + threadIdx.x;
+  const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
   if (k >= c.n) return;
   const float4 pk = P[k];
   const float4 uk = U[k];
@@ -416,7 +449,7 @@ __global__ void __launch_bounds__(kGather)
   struct PU {
     float4 p, u;
   };
-  visit_neighbours(
+  visit_neighbours<kBatch>(
       nc, k, [&](uint32_t j) { return PU{__ldg(&P[j]), __ldg(&U[j])}; },
       [&](const PU &d, bool valid) {
     const float4 pj = d.p;
@@ -437,12 +470,13 @@ __global__ void __launch_bounds__(kGather)
   PW[k] = make_float4(pk.x, pk.y, pk.z, wn);
 }
 
-__global__ void __launch_bounds__(kGather)
+template <int kBlock, int kBatch>
+__global__ void __launch_bounds__(kBlock)
     k_xsph_commit(const float4 *__restrict__ PW, const float4 *__restrict__ U,
                   const float4 *__restrict__ Wv, NbrCtx nc, PaperConsts c,
                   const uint32_t *__restrict__ ID2, float4 *__restrict__ X,
                   float4 *__restrict__ V, uint32_t *__restrict__ ID) {
-  const uint32_t k = blockIdx.x * kGather + threadIdx.x;
+  const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
   if (k >= c.n) return;
   const float4 pk = PW[k];
   const float4 uk = U[k];
@@ -451,7 +485,7 @@ __global__ void __launch_bounds__(kGather)
   struct PU {
     float4 p, u;
   };
-  visit_neighbours(
+  visit_neighbours<kBatch>(
       nc, k, [&](uint32_t j) { return PU{__ldg(&PW[j]), __ldg(&U[j])}; },
       [&](const PU &d, bool valid) {
     const float4 pj = d.p;
@@ -575,38 +609,77 @@ cudaError_t paper_reorder(const uint32_t *perm, const float4 *X,
   return cudaGetLastError();
 }
 
+// Launches KERNEL<threads, loads in flight> (or KERNEL<threads> for the list
+// builds) in the shape d.tune gives for KIND, between the tuner's events
+// when its timer is attached.
+#define PBF_GATHER_LAUNCH(KERNEL, KIND, ...)                                          \
+  do {                                                                                 \
+    const int slot_ = d.timer ? d.timer->begin(KIND, st) : -1;                         \
+    switch (d.tune.block[KIND] * kBatchCodes + d.tune.batch[KIND]) {                   \
+      case 0: KERNEL<64, 4><<<blocks_for(c.n, 64), 64, 0, st>>>(__VA_ARGS__); break;    \
+      case 1: KERNEL<64, 8><<<blocks_for(c.n, 64), 64, 0, st>>>(__VA_ARGS__); break;    \
+      case 2: KERNEL<128, 4><<<blocks_for(c.n, 128), 128, 0, st>>>(__VA_ARGS__); break; \
+      case 3: KERNEL<128, 8><<<blocks_for(c.n, 128), 128, 0, st>>>(__VA_ARGS__); break; \
+      case 4: KERNEL<256, 4><<<blocks_for(c.n, 256), 256, 0, st>>>(__VA_ARGS__); break; \
+      case 5: KERNEL<256, 8><<<blocks_for(c.n, 256), 256, 0, st>>>(__VA_ARGS__); break; \
+      default: return cudaErrorInvalidValue;                                           \
+    }                                                                                  \
+    if (d.timer) d.timer->end(slot_, st);                                              \
+  } while (0)
+
+#define PBF_BUILD_LAUNCH(KERNEL, KIND, ...)                                           \
+  do {                                                                                 \
+    const int slot_ = d.timer ? d.timer->begin(KIND, st) : -1;                         \
+    switch (d.tune.block[KIND]) {                                                      \
+      case 0: KERNEL<64><<<blocks_for(c.n, 64), 64, 0, st>>>(__VA_ARGS__); break;       \
+      case 1: KERNEL<128><<<blocks_for(c.n, 128), 128, 0, st>>>(__VA_ARGS__); break;    \
+      case 2: KERNEL<256><<<blocks_for(c.n, 256), 256, 0, st>>>(__VA_ARGS__); break;    \
+      default: return cudaErrorInvalidValue;                                           \
+    }                                                                                  \
+    if (d.timer) d.timer->end(slot_, st);                                              \
+  } while (0)
+
 cudaError_t paper_nbr_build(const DeviceState &d, const PaperConsts &c,
                             const uint16_t *sid, cudaStream_t st) {
-  k_nbr_build<<<blocks_for(c.n, kGather), kGather, 0, st>>>(d.P, make_ctx(d, c, sid), c, d.nbr,
-                                                           d.nbr_cnt);
+  PBF_BUILD_LAUNCH(k_nbr_build, kKindNbr, d.P, make_ctx(d, c, sid), c, d.nbr, d.nbr_cnt);
+  return cudaGetLastError();
+}
+
+cudaError_t paper_nbr_lambda(const DeviceState &d, const PaperConsts &c,
+                             const uint16_t *sid, cudaStream_t st) {
+  PBF_BUILD_LAUNCH(k_nbr_lambda, kKindNbrLambda, d.P, make_ctx(d, c, sid), c, d.nbr, d.nbr_cnt,
+                   d.Q, d.R);
   return cudaGetLastError();
 }
 
 cudaError_t paper_lambda(const DeviceState &d, const PaperConsts &c,
                          const uint16_t *sid, cudaStream_t st) {
-  k_lambda<<<blocks_for(c.n, kGather), kGather, 0, st>>>(d.P, make_ctx(d, c, sid), c, d.Q, d.R);
+  PBF_GATHER_LAUNCH(k_lambda, kKindLambda, d.P, make_ctx(d, c, sid), c, d.Q, d.R);
   return cudaGetLastError();
 }
 
 cudaError_t paper_delta(const DeviceState &d, const PaperConsts &c,
                         const uint16_t *sid, bool last, cudaStream_t st) {
-  k_delta<<<blocks_for(c.n, kGather), kGather, 0, st>>>(d.Q, make_ctx(d, c, sid), c, d.D, d.P, d.R, d.U,
-                                     last ? 1 : 0);
+  PBF_GATHER_LAUNCH(k_delta, kKindDelta, d.Q, make_ctx(d, c, sid), c, d.D, d.P, d.R, d.U,
+                    last ? 1 : 0);
   return cudaGetLastError();
 }
 
 cudaError_t paper_vorticity(const DeviceState &d, const PaperConsts &c,
                             const uint16_t *sid, cudaStream_t st) {
-  k_vorticity<<<blocks_for(c.n, kGather), kGather, 0, st>>>(d.P, d.U, make_ctx(d, c, sid), c, d.W, d.D);
+  PBF_GATHER_LAUNCH(k_vorticity, kKindVorticity, d.P, d.U, make_ctx(d, c, sid), c, d.W, d.D);
   return cudaGetLastError();
 }
 
 cudaError_t paper_xsph_commit(const DeviceState &d, const PaperConsts &c,
                               const uint16_t *sid, cudaStream_t st) {
-  k_xsph_commit<<<blocks_for(c.n, kGather), kGather, 0, st>>>(d.D, d.U, d.W, make_ctx(d, c, sid), c, d.ID2,
-                                           d.X, d.V, d.ID);
+  PBF_GATHER_LAUNCH(k_xsph_commit, kKindXsph, d.D, d.U, d.W, make_ctx(d, c, sid), c, d.ID2,
+                    d.X, d.V, d.ID);
   return cudaGetLastError();
 }
+
+#undef PBF_GATHER_LAUNCH
+#undef PBF_BUILD_LAUNCH
 
 cudaError_t gather_to_input_order(const float4 *X, const float4 *V,
                                   const uint32_t *ID, uint32_t n,

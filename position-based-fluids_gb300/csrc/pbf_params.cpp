@@ -228,3 +228,40 @@ void pbf_params_default(pbf_params *p) {
 }
 
 }  // extern "C"
+
+namespace pbf {
+
+void to_pbf_tuning(const GatherTuning &g, const double trial_ms[kGatherKinds], pbf_tuning *out) {
+  for (int k = 0; k < kGatherKinds; ++k) {
+    out->threads[k] = 64u << g.block[k];
+    out->batch[k] = 4u << g.batch[k];
+    out->trial_ms[k] = trial_ms ? (float)trial_ms[k] : 0.0f;
+  }
+  out->fuse_first = g.fuse_first;
+}
+
+int to_gather_tuning(const pbf_tuning &t, GatherTuning *out) {
+  GatherTuning g;
+  for (int k = 0; k < kGatherKinds; ++k) {
+    int bl = -1, nb = -1;
+    for (int c = 0; c < kBlockCodes; ++c)
+      if (t.threads[k] == (64u << c)) bl = c;
+    for (int c = 0; c < kBatchCodes; ++c)
+      if (t.batch[k] == (4u << c)) nb = c;
+    if (bl < 0 || nb < 0) {
+      set_error_message("tuning: threads must be 64, 128 or 256 and batch 4 or 8");
+      return PBF_ERR_INVALID;
+    }
+    g.block[k] = (uint8_t)bl;
+    g.batch[k] = (uint8_t)nb;
+  }
+  if (t.fuse_first > 1) {
+    set_error_message("tuning: fuse_first must be 0 or 1");
+    return PBF_ERR_INVALID;
+  }
+  g.fuse_first = (uint8_t)t.fuse_first;
+  *out = g;
+  return PBF_OK;
+}
+
+}  // namespace pbf

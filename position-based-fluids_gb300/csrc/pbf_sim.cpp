@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "pbf_host.hpp"
+#include "pbf_tune.hpp"
 
 using namespace pbf;
 
@@ -145,12 +146,17 @@ int launch_step(pbf_sim *s) {
     PBF_TRY_STATUS(mark(s, 0, "reorder", 1, &ev));
     const uint32_t iters = s->prm.solver_iterations;
     for (uint32_t it = 0; it < iters; ++it) {
-      if (it == 0) {
-        PBF_TRY(paper_nbr_build(d, s->pc, nullptr, st));
-        PBF_TRY_STATUS(mark(s, 1, "nbr_build", 1, &ev));
+      if (it == 0 && d.tune.fuse_first) {
+        PBF_TRY(paper_nbr_lambda(d, s->pc, nullptr, st));
+        PBF_TRY_STATUS(mark(s, 1, "nbr_lambda", 1, &ev));
+      } else {
+        if (it == 0) {
+          PBF_TRY(paper_nbr_build(d, s->pc, nullptr, st));
+          PBF_TRY_STATUS(mark(s, 1, "nbr_build", 1, &ev));
+        }
+        PBF_TRY(paper_lambda(d, s->pc, nullptr, st));
+        PBF_TRY_STATUS(mark(s, 1, "lambda", 1, &ev));
       }
-      PBF_TRY(paper_lambda(d, s->pc, nullptr, st));
-      PBF_TRY_STATUS(mark(s, 1, "lambda", 1, &ev));
       PBF_TRY(paper_delta(d, s->pc, nullptr, it + 1 == iters, st));
       PBF_TRY_STATUS(mark(s, 2, "delta", 1, &ev));
     }
@@ -507,9 +513,43 @@ int pbf_launches_per_step(const pbf_sim *s, uint32_t *launches) {
   const uint32_t it = s->prm.solver_iterations;
   const uint32_t sort = 1u /*scan*/ + s->plan.passes + 1u /*offsets*/;
   if (s->paper)
-    *launches = 1u /*predict+hash*/ + sort + 1u /*reorder*/ + 1u /*lists*/ + 2u * it + 2u;
+    *launches = 1u /*predict+hash*/ + sort + 1u /*reorder*/ + paper_first_launches(s->d) +
+                2u * it - 1u + 2u;
   else
     *launches = 1u + sort + 2u * it + 2u;
+  return PBF_OK;
+}
+
+int pbf_autotune(pbf_sim *s, uint32_t trial_steps, pbf_tuning *out) {
+  if (!ready(s)) return s ? PBF_ERR_STATE : PBF_ERR_INVALID;
+  if (trial_steps < 1 || trial_steps > 32) return PBF_ERR_INVALID;
+  double ms[kGatherKinds] = {0, 0, 0, 0, 0, 0};
+  if (s->paper) {
+    const bool timing = s->timing;
+    s->timing = false;
+    const int rc = paper_autotune(s->d, s->n, s->stream, trial_steps,
+                                  [&]() { return launch_step(s); }, ms);
+    s->timing = timing;
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+    if (rc != PBF_OK) return rc;
+    PBF_TRY_STATUS(check_device_error(s));
+  }
+  if (out) to_pbf_tuning(s->d.tune, ms, out);
+  return PBF_OK;
+}
+
+int pbf_get_tuning(const pbf_sim *s, pbf_tuning *out) {
+  if (!s || !out) return PBF_ERR_INVALID;
+  to_pbf_tuning(s->d.tune, nullptr, out);
+  return PBF_OK;
+}
+
+int pbf_set_tuning(pbf_sim *s, const pbf_tuning *t) {
+  if (!s || !t) return PBF_ERR_INVALID;
+  PBF_TRY_STATUS(to_gather_tuning(*t, &s->d.tune));
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  s->graph = nullptr;
   return PBF_OK;
 }
 
