@@ -25,6 +25,24 @@ Our arm prints one JSON line with:
 The working set (state, neighbour lists, sort buffers) is several hundred MB,
 larger than L2, so no flush runs between steps.
 
+  forms     (default) the batched and served workloads below, summarised:
+            value, vs the same scenes solved one by one on the plain path,
+            scene latency.
+Before warm-up each workload runs the launch-shape tuner on its own scenes
+(--no-tune keeps the defaults; results are bitwise the same either way).
+
+--workload batch: 256 independent dam breaks, N log-uniform 4,096..262,144,
+block aspect ratios in [0.5, 2], boxes twice the block extent, advanced
+together for 300 steps (one launch per kernel per step, CUDA graph); against
+each scene alone on the plain path.
+--workload serve: a seeded Poisson stream (mean 50 requests/s) of dam-break
+solves, N log-uniform 8,192..524,288, 100..1000 steps each, submitted in
+real time for --serve-seconds to the request loop (continuous batching
+under a 120 GB HBM budget); p50/p99 completion latency; against the same
+requests solved one at a time on the plain path.
+--save-state / --load-state write and resume the single scene's state (for
+profiling a late state of the simulation).
+
 --impl reference times the reference's own CPU implementation on the same
 workload and prints the same line with "impl": "reference".
 Under torchrun (N > 1) every rank runs an independent replica of the scene
@@ -347,6 +365,8 @@ def run_ours(args) -> int:
             "clocks": clock_summary,
             "cpu_baseline": cpu,
         }
+        if args.forms == "all" and world == 1:
+            line["forms"] = form_summaries(args)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -382,7 +402,7 @@ def plain_one_by_one(pbf, scenes, steps: int, sample_steps: int, ext_stream_of):
     return step_s, setup_s
 
 
-def run_batch(args) -> int:
+def run_batch(args, emit: bool = True):
     """256 independent dam-break scenes of log-uniform sizes advanced together
     (one launch per kernel per step, CUDA-graph step) against the same scenes
     solved one at a time on the plain path."""
@@ -474,10 +494,11 @@ def run_batch(args) -> int:
             "speedup_vs_plain": (value / plain["value"]) if plain else None,
             "clocks": clocks.summary(),
         }
-        print(json.dumps(line), flush=True)
+        if emit:
+            print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
-    return 0
+    return line if not emit else 0
 
 
 def fifo_latencies(arrivals, service):
@@ -491,7 +512,7 @@ def fifo_latencies(arrivals, service):
     return lat, t
 
 
-def run_serve(args) -> int:
+def run_serve(args, emit: bool = True):
     """A seeded Poisson stream of dam-break solves (mean 50 per second, N
     log-uniform 8,192..524,288, 100..1000 steps) submitted in real time to
     the request loop (continuous batching under a 120 GB HBM budget), against
@@ -580,8 +601,39 @@ def run_serve(args) -> int:
         "speedup_vs_plain": (value / plain["value"]) if plain else None,
         "clocks": clocks.summary(),
     }
+    if not emit:
+        return line
     print(json.dumps(line), flush=True)
     return 0
+
+
+def form_summaries(args) -> dict:
+    """The batched and served workloads, summarised for the headline line."""
+    import copy
+
+    out = {}
+    a = copy.copy(args)
+    a.steps = 300
+    b = run_batch(a, emit=False)
+    if b:
+        out["batched"] = {
+            "workload": b["config"]["workload"], "scenes": b["config"]["scenes"],
+            "particles": b["config"]["particles"], "steps": b["steps"], "value": b["value"],
+            "unit": b["unit"], "ms_per_step": b["ms_per_step"], "e2e": b["e2e"]["value"],
+            "plain_one_by_one": b["plain_one_by_one"]["value"] if b["plain_one_by_one"] else None,
+            "speedup_vs_plain": b["speedup_vs_plain"], "scene_latency_s": b["scene_latency_s"]["p50"],
+            "gpu_launches": b["gpu_launches"], "clocks": b["clocks"]}
+    s = run_serve(copy.copy(args), emit=False)
+    out["served"] = {
+        "workload": s["config"]["workload"], "requests": s["config"]["requests"],
+        "arrival_window_s": s["config"]["arrival_window_s"], "value": s["value"], "unit": s["unit"],
+        "scene_latency_s": s["scene_latency_s"],
+        "plain_one_by_one": ({"value": s["plain_one_by_one"]["value"],
+                              "scene_latency_s": s["plain_one_by_one"]["scene_latency_s"]}
+                             if s["plain_one_by_one"] else None),
+        "speedup_vs_plain": s["speedup_vs_plain"], "hbm_budget_bytes": s["config"]["hbm_budget_bytes"],
+        "gpu_launches": s["gpu_launches"], "clocks": s["clocks"]}
+    return out
 
 
 def main() -> int:
@@ -601,6 +653,9 @@ def main() -> int:
                     help="timed steps per scene of the one-by-one plain comparison")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-by-one plain comparison")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--forms", choices=["all", "none"], default="all",
+                    help="single workload: also run the batched and served workloads and "
+                         "summarise them in the line (one GPU only)")
     ap.add_argument("--save-state", default=None,
                     help="single scene: write the state after the warm-up and timed steps (.npz)")
     ap.add_argument("--load-state", default=None,
