@@ -239,6 +239,27 @@ int pbf_get_cells(pbf_sim *sim, uint32_t *hash, uint32_t *perm,
                   int32_t *ranges);
 int pbf_destroy(pbf_sim *sim);
 
+/* ------------------------------------------------- headless rendering */
+/* The reference's particle drawing (src/visual/visual.cpp:86-125,217-330,
+ * src/shaders/particlevertex.glsl, particlefragment.glsl) as CUDA kernels
+ * writing an image instead of a window: a spherical camera around `target`
+ * (angles in degrees, negative distance as the reference uses), a
+ * perspective projection, point sprites of 200 / clip.w pixels shaded as
+ * spheres lit from (1,1,1), colour (|v|, |v|, 1), depth test "less" with
+ * ties to the lower input index, background 0.05 grey. */
+typedef struct pbf_camera {
+  float phi_deg, theta_deg, distance;
+  float target[3];
+  float fovy_deg, znear, zfar;
+  float max_point_size;           /* cap on a sprite's diameter, pixels   */
+} pbf_camera;
+/* The reference's initial camera for this box. */
+void pbf_camera_default(const pbf_params *p, pbf_camera *out);
+/* Renders the current state into rgb (width * height * 3 bytes, rows top
+ * first).  Synchronous. */
+int pbf_render(pbf_sim *sim, const pbf_camera *cam, uint32_t width,
+               uint32_t height, uint8_t *rgb);
+
 /* ------------------------------------------------------ batched scenes */
 /* Many independent scenes advanced together (no counterpart in the
  * reference, which runs one scene): one sort over scene-major keys (scene s
@@ -280,6 +301,9 @@ int pbf_batch_autotune(pbf_batch *b, uint32_t trial_steps, pbf_tuning *out);
 int pbf_batch_get_tuning(const pbf_batch *b, pbf_tuning *out);
 int pbf_batch_set_tuning(pbf_batch *b, const pbf_tuning *tuning);
 int pbf_batch_destroy(pbf_batch *b);
+/* pbf_render for one scene of a batch (the scene's own box). */
+int pbf_batch_render_scene(pbf_batch *b, uint32_t scene_id, const pbf_camera *cam,
+                           uint32_t width, uint32_t height, uint8_t *rgb);
 
 /* ------------------------------------------------------- served scenes */
 /* A request loop over one batch (continuous batching).  Requests (a scene

@@ -99,6 +99,14 @@ PARTICLE_DTYPE = np.dtype([("m", np.float32), ("x", np.float32, 3), ("v", np.flo
 assert PARTICLE_DTYPE.itemsize == C.sizeof(Particle)
 
 
+class Camera(C.Structure):
+    """pbf_camera: the reference's spherical camera (src/visual/visual.cpp:86-125)."""
+
+    _fields_ = [("phi_deg", C.c_float), ("theta_deg", C.c_float), ("distance", C.c_float),
+                ("target", C.c_float * 3), ("fovy_deg", C.c_float), ("znear", C.c_float),
+                ("zfar", C.c_float), ("max_point_size", C.c_float)]
+
+
 class Tuning(C.Structure):
     """pbf_tuning: launch shape of the gather passes (list build, fused list
     build + first lambda, lambda, delta-p, vorticity, XSPH)."""
@@ -183,6 +191,9 @@ def lib():
             "pbf_get_cells": ([vp, vp, vp, vp], i32),
             "pbf_destroy": ([vp], i32),
             "pbf_autotune": ([vp, u32, C.POINTER(Tuning)], i32),
+            "pbf_camera_default": ([pp, C.POINTER(Camera)], None),
+            "pbf_render": ([vp, C.POINTER(Camera), u32, u32, vp], i32),
+            "pbf_batch_render_scene": ([vp, u32, C.POINTER(Camera), u32, u32, vp], i32),
             "pbf_get_tuning": ([vp, C.POINTER(Tuning)], i32),
             "pbf_set_tuning": ([vp, C.POINTER(Tuning)], i32),
             "pbf_batch_autotune": ([vp, u32, C.POINTER(Tuning)], i32),
@@ -441,6 +452,14 @@ class Simulation:
     def set_graph(self, enable: bool):
         _check(lib().pbf_set_graph(self._h, int(enable)), "pbf_set_graph")
 
+    def render(self, camera: Camera | None = None, width: int = 640, height: int = 480) -> np.ndarray:
+        """The current state drawn as the reference's renderer draws it:
+        (height, width, 3) uint8, top row first."""
+        cam = camera if camera is not None else default_camera(self.params)
+        img = np.zeros((height, width, 3), np.uint8)
+        _check(lib().pbf_render(self._h, C.byref(cam), width, height, _ptr(img)), "pbf_render")
+        return img
+
     def autotune(self, trial_steps: int = 3) -> Tuning:
         """Picks the fastest launch shape of each gather pass on this scene
         (the state is restored; results are unchanged)."""
@@ -532,6 +551,14 @@ class Batch:
         t = Tuning()
         _check(lib().pbf_batch_autotune(self._h, trial_steps, C.byref(t)), "pbf_batch_autotune")
         return t
+
+    def render_scene(self, scene_id: int, params: Params, camera: Camera | None = None,
+                     width: int = 640, height: int = 480) -> np.ndarray:
+        cam = camera if camera is not None else default_camera(params)
+        img = np.zeros((height, width, 3), np.uint8)
+        _check(lib().pbf_batch_render_scene(self._h, scene_id, C.byref(cam), width, height, _ptr(img)),
+               "pbf_batch_render_scene")
+        return img
 
     def tuning(self) -> Tuning:
         t = Tuning()
@@ -633,6 +660,21 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def default_camera(params: Params) -> Camera:
+    """The reference's initial camera for the box of `params`."""
+    cam = Camera()
+    lib().pbf_camera_default(C.byref(params), C.byref(cam))
+    return cam
+
+
+def write_ppm(path, img: np.ndarray) -> None:
+    """Binary PPM (P6) of an (H, W, 3) uint8 image."""
+    h, w, _ = img.shape
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (w, h))
+        f.write(np.ascontiguousarray(img, np.uint8).tobytes())
 
 
 # ------------------------------------------------------------------ operators

@@ -456,6 +456,23 @@ int pbf_batch_set_tuning(pbf_batch *b, const pbf_tuning *t) {
   return PBF_OK;
 }
 
+int pbf_batch_render_scene(pbf_batch *b, uint32_t scene_id, const pbf_camera *cam,
+                           uint32_t width, uint32_t height, uint8_t *rgb) {
+  if (!b || !cam || !rgb) return PBF_ERR_INVALID;
+  const int i = find_scene(b, scene_id);
+  if (i < 0) return PBF_ERR_NOT_FOUND;
+  if (b->dirty) PBF_TRY_STATUS(apply_layout(b));
+  const SceneRec &s = b->scenes[i];
+  const uint32_t pb = s.desc.p_begin;
+  pbf_params box = b->solver;
+  box.x_min = s.desc.gmin[0]; box.y_min = s.desc.gmin[1]; box.z_min = s.desc.gmin[2];
+  box.x_max = s.desc.gmin[0] + s.desc.clen[0] * (float)s.desc.ncell[0];
+  box.y_max = s.desc.gmin[1] + s.desc.clen[1] * (float)s.desc.ncell[1];
+  box.z_max = s.desc.gmin[2] + s.desc.clen[2] * (float)s.desc.ncell[2];
+  return render_particles(b->d.X + pb, b->d.ID + pb, s.n, box, *cam, width, height, rgb,
+                          b->stream);
+}
+
 int pbf_batch_destroy(pbf_batch *b) {
   if (!b) return PBF_OK;
   if (b->stream) cudaStreamSynchronize(b->stream);

@@ -44,4 +44,10 @@ void batch_capacity(const pbf_batch *b, uint32_t *scenes, uint32_t *particles,
 void to_pbf_tuning(const GatherTuning &g, const double trial_ms[kGatherKinds], pbf_tuning *out);
 int to_gather_tuning(const pbf_tuning &t, GatherTuning *out);
 
+// Renders n particles (X: position, .w = |v|; ID: input index of each slot,
+// or null when slot = input index) of the box of `prm` into rgb (host).
+int render_particles(const float4 *X, const uint32_t *ID, uint32_t n, const pbf_params &prm,
+                     const pbf_camera &cam, uint32_t width, uint32_t height, uint8_t *rgb,
+                     cudaStream_t st);
+
 }  // namespace pbf

@@ -520,6 +520,14 @@ int pbf_launches_per_step(const pbf_sim *s, uint32_t *launches) {
   return PBF_OK;
 }
 
+int pbf_render(pbf_sim *s, const pbf_camera *cam, uint32_t width, uint32_t height,
+               uint8_t *rgb) {
+  if (!ready(s)) return s ? PBF_ERR_STATE : PBF_ERR_INVALID;
+  if (!cam || !rgb) return PBF_ERR_INVALID;
+  return render_particles(s->d.X, s->paper ? s->d.ID : nullptr, s->n, s->prm, *cam, width,
+                          height, rgb, s->stream);
+}
+
 int pbf_autotune(pbf_sim *s, uint32_t trial_steps, pbf_tuning *out) {
   if (!ready(s)) return s ? PBF_ERR_STATE : PBF_ERR_INVALID;
   if (trial_steps < 1 || trial_steps > 32) return PBF_ERR_INVALID;

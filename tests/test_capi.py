@@ -224,3 +224,34 @@ def test_scenes_shapes(pbf):
     assert x.min() >= -1e-3 + m and x[:, 0].max() <= 6.4 - m + 1e-3
     b = pbf.scenes.mixed_batch(16)
     assert len(b) == 16 and all(4096 * 0.9 <= s.n <= 262144 * 1.1 for s in b)
+
+
+def test_ppm_writer(pbf, tmp_path):
+    img = np.zeros((3, 4, 3), np.uint8)
+    img[0, 0] = (255, 0, 0)
+    p = tmp_path / "x.ppm"
+    pbf.write_ppm(p, img)
+    data = p.read_bytes()
+    assert data.startswith(b"P6\n4 3\n255\n") and len(data) == len(b"P6\n4 3\n255\n") + 36
+
+
+def test_render_restatement_single_particle(pbf):
+    """The renderer's checker: one particle at the box centre seen by the
+    reference's initial camera is a disc at the image centre, (|v|, |v|, 1)
+    at its middle (normal towards the camera), on the 0.05 grey background."""
+    from oracle import render as oracle_render
+
+    sc = pbf.scenes.dam_break((2, 2, 2), (0.8, 0.8, 0.8), seed=1)
+    cam = pbf.default_camera(sc.params)
+    assert cam.theta_deg == 20.0 and cam.fovy_deg == 45.0 and abs(cam.distance + 1.6) < 1e-6
+    cam.max_point_size = 256.0
+    pos = np.array([[0.4, 0.4, 0.4, 0.5]], np.float32)
+    img = oracle_render.render(pos, sc.params, cam, 400, 300)
+    assert tuple(img[0, 0]) == (13, 13, 13)
+    c = img[150, 200].astype(int)
+    assert abs(c[0] - 128) <= 2 and c[0] == c[1] and c[2] == 255
+    covered = (img != 13).any(axis=2)  # unlit parts of the sphere are black, not background
+    ys, xs = np.nonzero(covered)
+    assert abs(xs.mean() - 199.5) < 1.5 and abs(ys.mean() - 149.5) < 1.5
+    # 200 / w pixels across, w = the distance along the view axis (1.6 m)
+    assert abs((xs.max() - xs.min() + 1) - 200 / 1.6) <= 2
