@@ -67,6 +67,7 @@ struct pbf_batch {
   SortPlan plan;
   bool dirty = true;
   cudaGraphExec_t graph = nullptr;
+  bool graph_stale = false;
   std::vector<SceneDesc> table;
 };
 
@@ -118,11 +119,9 @@ int apply_layout(pbf_batch *b) {
   if (!b->scenes.empty()) {
     PBF_TRY(cudaMemcpyAsync(d.scenes, b->table.data(), b->table.size() * sizeof(SceneDesc),
                             cudaMemcpyHostToDevice, b->stream));
-    for (size_t i = 0; i < b->scenes.size(); ++i)
-      PBF_TRY(fill_u16(d.sid + b->table[i].p_begin, b->scenes[i].n, (uint16_t)i, b->stream));
+    PBF_TRY(scene_ids(d.scenes, (uint32_t)b->scenes.size(), p, d.sid, b->stream));
   }
-  if (b->graph) cudaGraphExecDestroy(b->graph);
-  b->graph = nullptr;
+  b->graph_stale = true;  // same kernels, new sizes: updated in place at the next step
   b->dirty = false;
   return PBF_OK;
 }
@@ -338,7 +337,7 @@ int pbf_batch_step(pbf_batch *b, uint32_t nsteps) {
   if (!b) return PBF_ERR_INVALID;
   if (b->dirty) PBF_TRY_STATUS(apply_layout(b));
   if (b->n_total == 0) return PBF_OK;
-  if (!b->graph) {
+  if (!b->graph || b->graph_stale) {
     cudaGraph_t g = nullptr;
     PBF_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     const int rc = launch_batch_step(b);
@@ -348,12 +347,27 @@ int pbf_batch_step(pbf_batch *b, uint32_t nsteps) {
       return rc;
     }
     if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture");
-    const cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
+    // A layout change keeps the kernels and only changes their arguments and
+    // grid sizes, so the executable graph is usually updated in place; a
+    // different topology (another number of radix passes) re-instantiates.
+    bool updated = false;
+    if (b->graph) {
+      cudaGraphExecUpdateResultInfo info;
+      updated = cudaGraphExecUpdate(b->graph, g, &info) == cudaSuccess;
+      if (!updated) {
+        cudaGetLastError();
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+      }
+    }
+    cudaError_t ie = cudaSuccess;
+    if (!updated) ie = cudaGraphInstantiate(&b->graph, g, 0);
     cudaGraphDestroy(g);
     if (ie != cudaSuccess) {
       b->graph = nullptr;
       return cuda_status(ie, "cudaGraphInstantiate");
     }
+    b->graph_stale = false;
   }
   for (uint32_t k = 0; k < nsteps; ++k) PBF_TRY(cudaGraphLaunch(b->graph, b->stream));
   return PBF_OK;

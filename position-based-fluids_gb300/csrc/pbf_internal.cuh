@@ -206,8 +206,9 @@ struct DeviceState {
   GatherTimer *timer = nullptr;
 };
 
-// Fills dst[0, n) with `value`.
-cudaError_t fill_u16(uint16_t *dst, uint32_t n, uint16_t value, cudaStream_t st);
+// Scene of every sorted slot of a batch from its scene table (device).
+cudaError_t scene_ids(const SceneDesc *scenes, uint32_t nscenes, uint32_t n, uint16_t *sid,
+                      cudaStream_t st);
 // dst[i] = i for i in [0, n).
 cudaError_t iota_range(uint32_t *dst, uint32_t n, cudaStream_t st);
 

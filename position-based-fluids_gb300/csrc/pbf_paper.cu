@@ -559,9 +559,19 @@ __global__ void k_iota(uint32_t *__restrict__ dst, uint32_t n) {
   if (k < n) dst[k] = k;
 }
 
-__global__ void k_fill_u16(uint16_t *__restrict__ dst, uint32_t n, uint16_t value) {
+// sid[k] = the scene whose [p_begin, p_end) holds slot k (scenes in slot
+// order, found by binary search on p_begin).
+__global__ void k_scene_ids(const SceneDesc *__restrict__ scenes, uint32_t nscenes, uint32_t n,
+                            uint16_t *__restrict__ sid) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) dst[k] = value;
+  if (k >= n) return;
+  uint32_t lo = 0, hi = nscenes - 1u;  // largest s with p_begin <= k
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1u) >> 1;
+    if (scenes[mid].p_begin <= k) lo = mid;
+    else hi = mid - 1u;
+  }
+  sid[k] = (uint16_t)lo;
 }
 
 inline uint32_t blocks_for(uint64_t n, uint32_t t) {
@@ -714,10 +724,12 @@ cudaError_t iota_range(uint32_t *dst, uint32_t n, cudaStream_t st) {
   return iota_u32(dst, n, st);
 }
 
-cudaError_t fill_u16(uint16_t *dst, uint32_t n, uint16_t value, cudaStream_t st) {
-  if (n == 0) return cudaSuccess;
-  k_fill_u16<<<blocks_for(n, 256), 256, 0, st>>>(dst, n, value);
+cudaError_t scene_ids(const SceneDesc *scenes, uint32_t nscenes, uint32_t n, uint16_t *sid,
+                      cudaStream_t st) {
+  if (n == 0 || nscenes == 0) return cudaSuccess;
+  k_scene_ids<<<blocks_for(n, 256), 256, 0, st>>>(scenes, nscenes, n, sid);
   return cudaGetLastError();
 }
+
 
 }  // namespace pbf
