@@ -236,6 +236,45 @@ def run_reference(args) -> int:
     return 0
 
 
+def ref_equations_run(pbf, sc, args) -> dict:
+    """The same scene through the GPU path in REF_COMPAT mode (the
+    reference's own equations, bit-exact with its kernels): the like-for-like
+    figure beside the reference arm, which runs those equations on the CPU."""
+    import torch
+
+    p = sc.params.copy()
+    p.mode = pbf.MODE_REF_COMPAT
+    warm, steps = 2, 20  # the first 22 steps, the sample the CPU reference arm times
+    with pbf.Simulation(p, sc.particles) as sim:
+        sim.init()
+        sim.initCells()
+        sim.step(warm)
+        ext = torch.cuda.ExternalStream(sim.stream())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        sim.step(steps, sync=False)
+        e1.record(ext)
+        e1.synchronize()
+        sim.sync()
+        t = e0.elapsed_time(e1) / 1e3
+        finite = bool(np.isfinite(sim.dumpData()[0]).all())
+        launches = sim.launches_per_step()
+    first_bad = None
+    if not finite:  # which step first leaves the finite range (untimed)
+        with pbf.Simulation(p, sc.particles) as sim:
+            sim.init()
+            for k in range(1, warm + steps + 1):
+                sim.step(1)
+                if not np.isfinite(sim.dumpData()[0]).all():
+                    first_bad = k
+                    break
+    return {"value": sc.n * ITERATIONS * steps / t, "unit": UNIT, "ms_per_step": t / steps * 1e3,
+            "steps": steps, "warmup": warm, "gpu_launches": launches * steps, "finite": finite,
+            "first_nonfinite_step": first_bad,
+            "equations": "reference kernels' equations (REF_COMPAT), device-resident, CUDA graph"}
+
+
 def run_ours(args) -> int:
     import torch
 
@@ -342,6 +381,7 @@ def run_ours(args) -> int:
         _, cpu = cpu_reference_run(budget_s=args.cpu_budget)
 
     sim.close()
+    ref_eq = ref_equations_run(pbf, sc, args) if world == 1 else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -364,6 +404,7 @@ def run_ours(args) -> int:
             "kernel_ms_per_step": {k: v[0] / kt_steps for k, v in kt.items()},
             "clocks": clock_summary,
             "cpu_baseline": cpu,
+            "ref_equations": ref_eq,
         }
         if args.forms == "all" and world == 1:
             line["forms"] = form_summaries(args)
