@@ -218,30 +218,11 @@ __global__ void __launch_bounds__(kSortThreads)
 // off[c] = number of sorted keys < c, for c in [0, ncells]: one thread per
 // cell, binary search over the sorted keys.  Neighbouring cells search
 // neighbouring key ranges, so the probes of a warp share cache lines.
-__global__ void __launch_bounds__(256)
-    k_cell_offsets(const uint32_t *__restrict__ skeys, uint32_t n, uint32_t ncells,
-                   uint32_t *__restrict__ off) {
-  // The block's cells [c0, c1] have their offsets between lower_bound(c0)
-  // and lower_bound(c1): two searches over all keys bound the block, then
-  // each thread searches only that range (a few levels instead of log2 n).
-  __shared__ uint32_t s_bound[2];
-  const uint32_t c0 = blockIdx.x * blockDim.x;
-  const uint32_t c1 = min(c0 + blockDim.x - 1u, ncells);
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  if (warp < 2 && lane == 0) {
-    const uint32_t target = warp == 0 ? c0 : c1;
-    uint32_t lo = 0, hi = n;
-    while (lo < hi) {
-      const uint32_t mid = lo + ((hi - lo) >> 1);
-      if (__ldg(&skeys[mid]) < target) lo = mid + 1;
-      else hi = mid;
-    }
-    s_bound[warp] = lo;
-  }
-  __syncthreads();
-  const uint32_t c = c0 + threadIdx.x;
+__global__ void k_cell_offsets(const uint32_t *__restrict__ skeys, uint32_t n,
+                               uint32_t ncells, uint32_t *__restrict__ off) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c > ncells) return;
-  uint32_t lo = s_bound[0], hi = s_bound[1];
+  uint32_t lo = 0, hi = n;
   while (lo < hi) {
     const uint32_t mid = lo + ((hi - lo) >> 1);
     if (__ldg(&skeys[mid]) < c) lo = mid + 1;
