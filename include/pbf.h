@@ -134,6 +134,18 @@ int pbf_read_config(const char *path, pbf_params *out);
  * particles parsed so far and a warning, as in the reference. */
 int pbf_read_particles(const char *path, pbf_particle **out, uint32_t *n);
 void pbf_free(void *ptr);
+/* Also reads the binary particle format (detected by its "PBFB" magic):
+ * u32 version 1, u64 count, count pbf_particle records, little-endian. */
+/* Writers: the .in text format above (values printed to round-trip float32
+ * exactly), the binary format, a .par file with every key (reference keys
+ * and the extension keys), and a legacy binary VTK POLYDATA file of the
+ * dumpData arrays (points, |v| as "speed", velocity vectors).  No
+ * reference counterpart (the reference reads scenarios only; its
+ * part_out_* / vtk_out_* keys are parsed but unused). */
+int pbf_write_particles(const char *path, const pbf_particle *p, uint32_t n);
+int pbf_write_particles_bin(const char *path, const pbf_particle *p, uint32_t n);
+int pbf_write_config(const char *path, const pbf_params *p);
+int pbf_write_vtk(const char *path, const float *pos4, const float *vel4, uint32_t n);
 /* DataLoader::getPathFor* (src/DataLoader.cpp:20-31) with an explicit root
  * instead of the executable's directory: root/data/<kind>s/<name> for kind
  * "scenario", "kernel", "shader" or "texture". */

@@ -165,6 +165,10 @@ def lib():
             "pbf_read_config": ([C.c_char_p, pp], i32),
             "pbf_read_particles": ([C.c_char_p, C.POINTER(vp), C.POINTER(u32)], i32),
             "pbf_free": ([vp], None),
+            "pbf_write_particles": ([C.c_char_p, vp, u32], i32),
+            "pbf_write_particles_bin": ([C.c_char_p, vp, u32], i32),
+            "pbf_write_config": ([C.c_char_p, pp], i32),
+            "pbf_write_vtk": ([C.c_char_p, vp, vp, u32], i32),
             "pbf_data_path": ([C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_size_t], i32),
             "pbf_generate_block": ([vp, u32, u32, u32, f32, f32, f32, C.c_uint64, vp], i32),
             "pbf_create": ([pp, vp, u32, C.POINTER(vp)], i32),
@@ -274,6 +278,26 @@ def read_particles(path) -> np.ndarray:
         C.memmove(out.ctypes.data, buf, n.value * PARTICLE_DTYPE.itemsize)
         lib().pbf_free(buf)
     return out
+
+
+def write_particles(path, particles: np.ndarray, binary: bool = False) -> None:
+    """A .in file (text, the reference's PartReader format) or, with
+    binary=True, the binary particle format read_particles also accepts."""
+    ps = np.ascontiguousarray(particles, PARTICLE_DTYPE)
+    fn = lib().pbf_write_particles_bin if binary else lib().pbf_write_particles
+    _check(fn(str(path).encode(), _ptr(ps), int(ps.shape[0])), "write_particles")
+
+
+def write_config(path, params: Params) -> None:
+    """A .par file with every key (reference keys and extension keys)."""
+    _check(lib().pbf_write_config(str(path).encode(), C.byref(params)), "write_config")
+
+
+def write_vtk(path, pos4: np.ndarray, vel4: np.ndarray) -> None:
+    """Legacy binary VTK POLYDATA of dumpData-layout arrays."""
+    pos = np.ascontiguousarray(pos4, np.float32).reshape(-1, 4)
+    vel = np.ascontiguousarray(vel4, np.float32).reshape(-1, 4)
+    _check(lib().pbf_write_vtk(str(path).encode(), _ptr(pos), _ptr(vel), int(pos.shape[0])), "write_vtk")
 
 
 def data_path(root, kind: str, name: str) -> str:

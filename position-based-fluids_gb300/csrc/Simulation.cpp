@@ -4,8 +4,10 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <iostream>
 #include <numeric>
+#include <thread>
 
 namespace pbf {
 
@@ -77,11 +79,89 @@ void Simulation::setWaveGenerator(const double value) {
   check(pbf_set_wave(sim_, (float)value), "Simulation::setWaveGenerator");
 }
 
+namespace {
+
+// Two pinned buffer pairs; a snapshot copies the state into the next pair
+// (waiting for that pair's previous file to be written) and hands the file
+// write to a thread.
+class SnapshotWriter {
+ public:
+  SnapshotWriter(pbf_sim *sim, uint32_t n) : sim_(sim), n_(n) {}
+  ~SnapshotWriter() { finish(); for (auto &s : slots_) release(s); }
+
+  void take(const std::string &path, bool vtk) {
+    Slot &s = slots_[next_];
+    next_ ^= 1;
+    if (s.writer.joinable()) s.writer.join();
+    check(s.status, "Runner snapshot");
+    if (!s.pos) {
+      void *p = nullptr, *v = nullptr;
+      check(pbf_host_alloc((size_t)n_ * 16, &p), "Runner snapshot");
+      check(pbf_host_alloc((size_t)n_ * 16, &v), "Runner snapshot");
+      s.pos = static_cast<float *>(p);
+      s.vel = static_cast<float *>(v);
+    }
+    check(pbf_dump_data_async(sim_, s.pos, s.vel), "Runner snapshot");
+    check(pbf_sync(sim_), "Runner snapshot");
+    s.writer = std::thread([&s, path, vtk, n = n_]() {
+      if (vtk) {
+        s.status = pbf_write_vtk(path.c_str(), s.pos, s.vel, n);
+        return;
+      }
+      std::vector<pbf_particle> ps(n);
+      for (uint32_t k = 0; k < n; ++k) {
+        pbf_particle &q = ps[k];
+        q.m = s.vel[4 * (size_t)k + 3];
+        for (int a = 0; a < 3; ++a) {
+          q.x[a] = s.pos[4 * (size_t)k + a];
+          q.v[a] = s.vel[4 * (size_t)k + a];
+          q.a[a] = 0.0f;
+        }
+      }
+      s.status = pbf_write_particles(path.c_str(), ps.data(), n);
+    });
+  }
+
+  void finish() {
+    for (auto &s : slots_)
+      if (s.writer.joinable()) s.writer.join();
+  }
+  void check_written() {
+    for (auto &s : slots_) check(s.status, "Runner snapshot");
+  }
+
+ private:
+  struct Slot {
+    float *pos = nullptr, *vel = nullptr;
+    std::thread writer;
+    int status = PBF_OK;
+  };
+  static void release(Slot &s) {
+    if (s.pos) pbf_host_free(s.pos);
+    if (s.vel) pbf_host_free(s.vel);
+    s.pos = s.vel = nullptr;
+  }
+  pbf_sim *sim_;
+  uint32_t n_;
+  Slot slots_[2];
+  int next_ = 0;
+};
+
+std::string frame_name(const char *base, const char *fallback, uint32_t frame, const char *ext) {
+  char buf[32];
+  std::snprintf(buf, sizeof buf, "%05u", frame);
+  return std::string(base[0] ? base : fallback) + buf + ext;
+}
+
+}  // namespace
+
 std::vector<double> Runner::run(const ConfigParameters &parameters,
                                 Simulation &simulation, bool waves,
                                 bool quiet) const {
   simulation.init();
   simulation.initCells();
+  SnapshotWriter snapshots(simulation.handle(), simulation.getNumberParticles());
+  uint64_t step_count = 0;
   const Float4 lo = simulation.getSizesMin(), hi = simulation.getSizesMax();
   float time = 0.0f, wave = 0.0f;
   std::vector<double> times;
@@ -100,7 +180,18 @@ std::vector<double> Runner::run(const ConfigParameters &parameters,
     }
     const auto t1 = std::chrono::steady_clock::now();
     times.push_back(std::chrono::duration<double>(t1 - t0).count());
+    ++step_count;
+    if (parameters.part_out_freq && step_count % parameters.part_out_freq == 0)
+      snapshots.take(frame_name(parameters.part_out_name_base, "part",
+                                (uint32_t)(step_count / parameters.part_out_freq), ".in"),
+                     false);
+    if (parameters.vtk_out_freq && step_count % parameters.vtk_out_freq == 0)
+      snapshots.take(frame_name(parameters.vtk_out_name_base, "vtk",
+                                (uint32_t)(step_count / parameters.vtk_out_freq), ".vtk"),
+                     true);
   } while (time <= parameters.time_end);
+  snapshots.finish();
+  snapshots.check_written();
   if (!quiet && !times.empty()) {
     const double sum = std::accumulate(times.begin(), times.end(), 0.0);
     const double mean = sum / times.size();

@@ -96,6 +96,12 @@ class Runner {
   // initCells, step until time_end (optionally with the sinusoidal wave
   // wall of src/Runner.cpp:91-104), then mean/median/std of the per-step
   // wall times.  Returns the per-step times in seconds.
+  //
+  // Snapshots: every part_out_freq steps the state is written as
+  // <part_out_name_base><frame>.in (the scenario format) and every
+  // vtk_out_freq steps as <vtk_out_name_base><frame>.vtk; frames count from
+  // 1, five digits.  The copy from the device goes into one of two pinned
+  // buffers and a host thread writes the file while stepping goes on.
   std::vector<double> run(const ConfigParameters &parameters,
                           Simulation &simulation, bool waves = false,
                           bool quiet = false) const;

@@ -104,6 +104,36 @@ def config_4m(seed: int = SEED) -> Scene:
                   "origins": [[m, m, m], [bx, m, m]], "seed": seed})
 
 
+def gen_grid(directory, name: str = "dam_coarse", h: float = 1.0, block_min=(10.0, 10.0, 10.0),
+             block_max=(20.0, 20.0, 20.0), domain=(0.0, 30.0)):
+    """The scenario pair tools/gen_grid.py writes (tools/gen_grid.py:1-49):
+    a lattice of round(extent / s) + 1 particles per axis at spacing
+    s = h / 2 from block_min (x outermost, unit mass, at rest) as <name>.in,
+    and <name>.par with a cubic domain, h-sized cells, time_end 1,
+    timestep 0.01 and restdensity = particles / block volume.  Returns the
+    two paths."""
+    from pathlib import Path
+
+    from . import write_config, write_particles
+
+    d = Path(directory)
+    s = h / 2
+    ext = [b - a for a, b in zip(block_min, block_max)]
+    counts = [int(round(e / s)) + 1 for e in ext]
+    ps = generate_block(block_min, *counts, s, 0.0, 1.0, 0)
+    write_particles(d / f"{name}.in", ps)
+    p = default_params()
+    p.part_input_file = f"{name}.in".encode()
+    p.time_end = 1.0
+    p.time_step_length = 0.01
+    p.x_min = p.y_min = p.z_min = domain[0]
+    p.x_max = p.y_max = p.z_max = domain[1]
+    p.x_n = p.y_n = p.z_n = float(int(round((domain[1] - domain[0]) / h)))
+    p.rest_density = ps.shape[0] / (ext[0] * ext[1] * ext[2])
+    write_config(d / f"{name}.par", p)
+    return d / f"{name}.in", d / f"{name}.par"
+
+
 def block_in_double_box(dims, seed: int, steps: int, name: str) -> Scene:
     """A dam-break block in the corner of a box twice the block's extent on
     every axis (rounded up to whole cells of size h)."""
