@@ -15,7 +15,7 @@
 //   P       predicted position x + d
 //   D       displacement d since the start of the step (kept apart from x so
 //           that positions round once per step, not once per iteration);
-//           after the last delta-p pass it holds (p, |vorticity|)
+//           the vorticity pass then reuses it for (p, |vorticity|)
 //   Q       (predicted position, lambda) as read by the delta-p pass
 //   U       (velocity, 1/rho) as read by the velocity passes
 //   W       (vorticity, |vorticity|)
@@ -27,16 +27,17 @@
 // Gather passes run one thread per sorted particle.  Neighbour lists hold
 // each neighbour as its 32-bit sorted slot, four per 16-byte word: group g of
 // particle k is nbr4[g*N + k], so a warp reads its particles' next four
-// neighbours with one coalesced load per thread, and the four neighbour loads
-// that follow are independent.  A particle whose set exceeds the list
-// capacity re-derives it from the cells and the step-start positions in
-// every pass instead (same order, same arithmetic).
+// neighbours with one coalesced load per thread, and the neighbour loads of
+// a batch (4 or 8 entries, a launch-shape choice) are independent.  A
+// particle whose set exceeds the list capacity re-derives it from the cells
+// and the step-start positions in every pass instead (same order, same
+// arithmetic).
 //
 // Measured on GB300 (1M-particle dam break after 500 steps, per step):
 // absolute 32-bit entries run 9% faster than 16-bit entries relative to a
 // per-tile table of row ranges -- the decode and the per-tile set-up cost
 // more issue slots than the larger lists cost DRAM time (the passes run at
-// ~15-20% of DRAM bandwidth); a variant that first staged each tile's
+// a third of DRAM bandwidth or less); a variant that first staged each tile's
 // neighbourhood into shared memory with cp.async.bulk ran 1.1-2x slower than
 // these L1 gathers; a persistent grid that kept neighbouring tiles on one SM
 // raised the L1 hit rate from 69% to 77% but ran 4% slower; four threads per
