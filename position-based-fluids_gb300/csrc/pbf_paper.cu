@@ -299,12 +299,30 @@ __global__ void __launch_bounds__(kBlock)
       const uint32_t row = s.cell_base + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
       const uint32_t a = __ldg(&nc.off[row + x0]);
       const uint32_t b = __ldg(&nc.off[row + x1 + 1]);
-      for (uint32_t j = a; j < b; j += 4) {
+      // whole groups of four candidates (loads at fixed offsets from one
+      // pointer, no per-load bound), then the last one to three
+      uint32_t j = a;
+      for (; j + 4u <= b; j += 4) {
+        const float4 *__restrict__ q = P + j;
         float4 d[4];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) d[e] = __ldg(&P[min(j + e, b - 1u)]);
+        for (int e = 0; e < 4; ++e) d[e] = __ldg(q + e);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
+          const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
+          const float r2 = rx * rx + ry * ry + rz * rz;
+          if (r2 > 0.0f && r2 < c.h2) {
+            if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j + e;
+            ++cnt;
+          }
+        }
+      }
+      if (j < b) {
+        float4 d[3];
+#pragma unroll
+        for (int e = 0; e < 3; ++e) d[e] = __ldg(&P[min(j + e, b - 1u)]);
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
           const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
           const float r2 = rx * rx + ry * ry + rz * rz;
           if (j + e < b && r2 > 0.0f && r2 < c.h2) {
@@ -353,12 +371,29 @@ __global__ void __launch_bounds__(kBlock)
       const uint32_t row = s.cell_base + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
       const uint32_t a = __ldg(&nc.off[row + x0]);
       const uint32_t b = __ldg(&nc.off[row + x1 + 1]);
-      for (uint32_t j = a; j < b; j += 4) {
+      uint32_t j = a;
+      for (; j + 4u <= b; j += 4) {
+        const float4 *__restrict__ q = P + j;
         float4 d[4];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) d[e] = __ldg(&P[min(j + e, b - 1u)]);
+        for (int e = 0; e < 4; ++e) d[e] = __ldg(q + e);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
+          const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
+          const float r2 = rx * rx + ry * ry + rz * rz;
+          if (r2 > 0.0f && r2 < c.h2) {
+            if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j + e;
+            ++cnt;
+            acc.add(rx, ry, rz, r2, c);
+          }
+        }
+      }
+      if (j < b) {
+        float4 d[3];
+#pragma unroll
+        for (int e = 0; e < 3; ++e) d[e] = __ldg(&P[min(j + e, b - 1u)]);
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
           const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
           const float r2 = rx * rx + ry * ry + rz * rz;
           if (j + e < b && r2 > 0.0f && r2 < c.h2) {
