@@ -422,6 +422,13 @@ int pbf_op_cell_offsets(const uint32_t *d_sorted_keys, uint32_t n,
                         uint32_t ncells, uint32_t *d_offsets, void *stream);
 /* The reference's cell ranges (init_cells.cl + find_cells.cl intent):
  * inclusive (first,last) int2 per cell, (-1,-1) if empty. */
+/* Failure-detection self-test: runs the radix sort's bounded look-back wait
+ * against a predecessor tile that never publishes, with `spin_limit` polls
+ * (1 .. 2^26).  The wait gives up, the kernel sets its error bit and
+ * returns; the call reports PBF_ERR_DEVICE with the device flag word in
+ * *device_flag, and the CUDA context stays usable.  PBF_OK would mean the
+ * wait did not give up.  No reference counterpart. */
+int pbf_selftest_bounded_wait(uint32_t spin_limit, uint32_t *device_flag);
 int pbf_op_find_cells(const uint32_t *d_offsets, uint32_t ncells,
                       int32_t *d_first_last, void *stream);
 

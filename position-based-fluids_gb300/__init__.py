@@ -210,6 +210,7 @@ def lib():
             "pbf_op_sort_pairs_noalloc": ([vp, vp, u32, u32, vp, vp, vp, vp], i32),
             "pbf_op_cell_offsets": ([vp, u32, u32, vp, vp], i32),
             "pbf_op_find_cells": ([vp, u32, vp, vp], i32),
+            "pbf_selftest_bounded_wait": ([u32, C.POINTER(u32)], i32),
             "pbf_batch_create": ([pp, u32, u32, u32, C.POINTER(vp)], i32),
             "pbf_batch_device_bytes": ([pp, u32, u32, u32], C.c_size_t),
             "pbf_batch_add_scene": ([vp, pp, vp, u32, C.POINTER(u32)], i32),

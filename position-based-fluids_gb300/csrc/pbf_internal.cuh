@@ -102,6 +102,11 @@ cudaError_t find_cells(const uint32_t *offsets, uint32_t ncells,
                        int32_t *first_last, cudaStream_t stream);
 cudaError_t cell_hash(const float4 *pred, uint32_t n, const SceneDesc &scene,
                       uint32_t *hash, cudaStream_t stream);
+// Runs the sort's bounded look-back wait against a predecessor that never
+// publishes (scratch: 2 * kRadix zeroed words); sets kDevErrLookback in *err
+// after spin_limit polls.
+cudaError_t wait_selftest(uint32_t *scratch, uint32_t spin_limit, uint32_t *err,
+                          cudaStream_t stream);
 // Number of kernel launches of one sort (histogram not included).
 uint32_t sort_pass_launches(const SortPlan &plan);
 

@@ -669,6 +669,33 @@ int pbf_op_cell_offsets(const uint32_t *d_sorted_keys, uint32_t n,
   return PBF_OK;
 }
 
+int pbf_selftest_bounded_wait(uint32_t spin_limit, uint32_t *device_flag) {
+  if (spin_limit == 0 || spin_limit > (1u << 26) || !device_flag) return PBF_ERR_INVALID;
+  cudaStream_t st = nullptr;
+  uint32_t *buf = nullptr;
+  int rc = PBF_OK;
+  auto cuda = [&](cudaError_t e, const char *where) {
+    if (e != cudaSuccess && rc == PBF_OK) rc = cuda_status(e, where);
+    return rc == PBF_OK;
+  };
+  *device_flag = 0;
+  if (cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "selftest") &&
+      cuda(cudaMalloc(&buf, (2 * kRadix + 1) * sizeof(uint32_t)), "selftest") &&
+      cuda(cudaMemsetAsync(buf, 0, (2 * kRadix + 1) * sizeof(uint32_t), st), "selftest") &&
+      cuda(wait_selftest(buf, spin_limit, buf + 2 * kRadix, st), "selftest") &&
+      cuda(cudaMemcpyAsync(device_flag, buf + 2 * kRadix, sizeof(uint32_t),
+                           cudaMemcpyDeviceToHost, st), "selftest"))
+    cuda(cudaStreamSynchronize(st), "selftest");
+  if (buf) cudaFree(buf);
+  if (st) cudaStreamDestroy(st);
+  if (rc != PBF_OK) return rc;
+  if (*device_flag) {
+    set_error_message("device error flag " + std::to_string(*device_flag));
+    return PBF_ERR_DEVICE;
+  }
+  return PBF_OK;
+}
+
 int pbf_op_find_cells(const uint32_t *d_offsets, uint32_t ncells,
                       int32_t *d_first_last, void *stream) {
   if (!d_offsets || !d_first_last) return PBF_ERR_INVALID;

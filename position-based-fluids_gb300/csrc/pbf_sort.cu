@@ -94,6 +94,40 @@ __global__ void __launch_bounds__(kSortThreads)
   }
 }
 
+// Exclusive prefix of digit d over tiles [0, tile) from the look-back
+// words, waiting for predecessors that have not published yet.  A wait of
+// more than spin_limit polls sets kDevErrLookback in *err and gives up
+// (returning what it has), so a kernel never spins without bound.
+__device__ __forceinline__ uint32_t lookback_prefix(uint32_t *lookback, uint32_t tile, uint32_t d,
+                                                    uint32_t spin_limit, uint32_t *err) {
+  uint32_t excl = 0;
+  int t = (int)tile - 1;
+  uint32_t spins = 0;
+  while (true) {
+    const uint32_t v = ld_volatile(&lookback[(size_t)t * kRadix + d]);
+    const uint32_t flag = v & ~kLbMask;
+    if (flag == 0u) {
+      if (++spins >= spin_limit) {
+        atomicOr(err, kDevErrLookback);
+        break;
+      }
+      if (spins > 64) __nanosleep(32);
+      continue;
+    }
+    excl += v & kLbMask;
+    if (flag == kLbInclusive || t == 0) break;
+    --t;
+  }
+  return excl;
+}
+
+// Runs the look-back wait of one digit against a predecessor tile that
+// never publishes (the words are zero): the wait must give up after
+// spin_limit polls and report through *err.
+__global__ void k_wait_selftest(uint32_t *lookback, uint32_t spin_limit, uint32_t *err) {
+  if (threadIdx.x == 0) lookback_prefix(lookback, 1u, 0u, spin_limit, err);
+}
+
 template <bool kIota>
 __global__ void __launch_bounds__(kSortThreads)
     k_onesweep(const uint32_t *__restrict__ keys_in,
@@ -165,23 +199,7 @@ __global__ void __launch_bounds__(kSortThreads)
     st_volatile(&lookback[d], kLbInclusive | tile_count);
   } else {
     st_volatile(&lookback[(size_t)tile * kRadix + d], kLbAggregate | tile_count);
-    int t = (int)tile - 1;
-    uint32_t spins = 0;
-    while (true) {
-      const uint32_t v = ld_volatile(&lookback[(size_t)t * kRadix + d]);
-      const uint32_t flag = v & ~kLbMask;
-      if (flag == 0u) {
-        if (++spins >= kSpinLimit) {
-          atomicOr(err, kDevErrLookback);
-          break;
-        }
-        if (spins > 64) __nanosleep(32);
-        continue;
-      }
-      excl += v & kLbMask;
-      if (flag == kLbInclusive || t == 0) break;
-      --t;
-    }
+    excl = lookback_prefix(lookback, tile, d, kSpinLimit, err);
     st_volatile(&lookback[(size_t)tile * kRadix + d],
                 kLbInclusive | ((excl + tile_count) & kLbMask));
   }
@@ -284,6 +302,12 @@ SortPlan make_sort_plan(uint32_t n, uint32_t key_bits) {
 }
 
 uint32_t sort_pass_launches(const SortPlan &plan) { return 2u + plan.passes; }
+
+cudaError_t wait_selftest(uint32_t *scratch, uint32_t spin_limit, uint32_t *err,
+                          cudaStream_t stream) {
+  k_wait_selftest<<<1, 32, 0, stream>>>(scratch, spin_limit, err);
+  return cudaGetLastError();
+}
 
 cudaError_t sort_clear(const SortPlan &plan, uint32_t *scratch,
                        cudaStream_t stream) {

@@ -255,3 +255,10 @@ def test_render_restatement_single_particle(pbf):
     assert abs(xs.mean() - 199.5) < 1.5 and abs(ys.mean() - 149.5) < 1.5
     # 200 / w pixels across, w = the distance along the view axis (1.6 m)
     assert abs((xs.max() - xs.min() + 1) - 200 / 1.6) <= 2
+
+
+def test_selftest_argument_checks(pbf):
+    flag = C.c_uint32()
+    assert pbf.lib().pbf_selftest_bounded_wait(0, C.byref(flag)) == pbf.ERR_INVALID
+    assert pbf.lib().pbf_selftest_bounded_wait(1 << 27, C.byref(flag)) == pbf.ERR_INVALID
+    assert pbf.lib().pbf_selftest_bounded_wait(100, None) == pbf.ERR_INVALID
