@@ -183,15 +183,17 @@ def reduce_max(dist, value: float, device=None) -> float:
     return float(t.item())
 
 
-def cpu_reference_run(n_steps_max: int = 50, budget_s: float = 15.0, threads: int = 0):
+def cpu_reference_run(n_steps_max: int = 50, budget_s: float = 15.0, threads: int = 0,
+                      scene=None):
     """Times the reference's own kernels (or the oracle restatement where
-    they are not built) on the 1M workload, one step at a time until
-    `budget_s` of CPU time is spent.  Returns (value, info)."""
+    they are not built) on the workload's scene (the 1M scene unless given),
+    one step at a time until `budget_s` of CPU time is spent.  Returns
+    (value, info)."""
     import oracle
     import __graft_entry__ as ge
 
     pbf = ge.load_package()
-    sc = pbf.scenes.config_1m()
+    sc = scene if scene is not None else pbf.scenes.config_1m()
     p = sc.params
     cfg = oracle.Config(p.x_min, p.x_max, p.y_min, p.y_max, p.z_min, p.z_max, p.x_n, p.y_n, p.z_n,
                         p.time_step_length, p.rest_density)
@@ -284,7 +286,7 @@ def run_ours(args) -> int:
     torch.cuda.set_device(local)
     dist = make_group(world, "nccl")
     pbf = ge.load_package()
-    sc = pbf.scenes.config_1m()
+    sc = pbf.scenes.config_4m() if args.workload == "large" else pbf.scenes.config_1m()
     n = sc.n
     sim = pbf.Simulation(sc.params, sc.particles)
     sim.init()
@@ -378,7 +380,7 @@ def run_ours(args) -> int:
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        _, cpu = cpu_reference_run(budget_s=args.cpu_budget)
+        _, cpu = cpu_reference_run(budget_s=args.cpu_budget, scene=sc)
 
     sim.close()
     ref_eq = ref_equations_run(pbf, sc, args) if world == 1 else None
@@ -387,8 +389,9 @@ def run_ours(args) -> int:
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "single_scene_1m", "particles": n, "cells": sc.params.ncells,
-                       "box": [6.4, 6.4, 6.4], "block": [128, 128, 64], "solver_iterations": ITERATIONS,
+            "config": {"workload": sc.name, "particles": n, "cells": sc.params.ncells,
+                       "box": sc.meta["box"], "blocks": sc.meta.get("blocks", [sc.meta.get("block")]),
+                       "solver_iterations": ITERATIONS,
                        "equations": "paper (relaxation 600, s_corr, XSPH, vorticity)",
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set larger than L2; no flush between steps",
@@ -406,7 +409,7 @@ def run_ours(args) -> int:
             "cpu_baseline": cpu,
             "ref_equations": ref_eq,
         }
-        if args.forms == "all" and world == 1:
+        if args.forms == "all" and world == 1 and args.workload == "single":
             line["forms"] = form_summaries(args)
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -684,7 +687,9 @@ def main() -> int:
                     help="timed steps (default 500 for the single scene, 300 for the batch)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["single", "batch", "serve"], default="single")
+    ap.add_argument("--workload", choices=["single", "large", "batch", "serve"], default="single",
+                    help="single: the 1M-particle scene (headline); large: the 4.2M-particle double "
+                         "dam break; batch; serve")
     ap.add_argument("--serve-seconds", type=float, default=6.0, help="arrival window of the served stream")
     ap.add_argument("--hbm-budget-gb", type=float, default=120.0, help="HBM budget of the request loop")
     ap.add_argument("--max-chunk", type=int, default=16, help="most batched steps per loop turn")
@@ -705,7 +710,7 @@ def main() -> int:
     if args.warmup < 3:
         args.warmup = 3
     if args.steps is None:
-        args.steps = 300 if args.workload == "batch" else 500
+        args.steps = {"batch": 300, "large": 200}.get(args.workload, 500)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch":
