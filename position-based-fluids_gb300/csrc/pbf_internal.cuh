@@ -56,6 +56,10 @@ struct RefConsts {
   uint32_t n;  // particles
 };
 
+// Grid of a grid-stride kernel with 256-thread CTAs: one full wave on the
+// 152 SMs of a GB300 (8 CTAs of 256 threads per SM).
+constexpr uint32_t kStrideCtas = 152u * 8u;
+
 // ------------------------------------------------------------------ sort --
 constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;

@@ -318,7 +318,7 @@ cudaError_t sort_clear(const SortPlan &plan, uint32_t *scratch,
 cudaError_t sort_histogram(const SortPlan &plan, const uint32_t *keys,
                            uint32_t *scratch, cudaStream_t stream) {
   if (plan.n == 0) return cudaSuccess;
-  const uint32_t blocks = min(blocks_for(plan.n, 256), 152u * 8u);
+  const uint32_t blocks = min(blocks_for(plan.n, 256), kStrideCtas);
   k_sort_histogram<<<blocks, 256, 0, stream>>>(keys, plan.n, plan.passes,
                                                scratch + plan.off_hist);
   return cudaGetLastError();
