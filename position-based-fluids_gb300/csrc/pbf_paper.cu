@@ -122,6 +122,12 @@ __device__ __forceinline__ void for_each_listed(const NbrCtx &c, uint32_t k, uin
   constexpr int kWords = kBatch / 4;
   for (uint32_t e0 = 0; e0 < cnt; e0 += kBatch) {
     uint32_t slot[kBatch];
+    // the next batch's list words, on their way to L2 while this one computes
+#pragma unroll
+    for (int w = 0; w < kWords; ++w) {
+      const uint32_t g = (e0 >> 2) + (uint32_t)(kWords + w);
+      if (4u * g < cnt) asm volatile("prefetch.global.L2 [%0];" ::"l"(&c.nbr4[(size_t)g * c.n + k]));
+    }
 #pragma unroll
     for (int w = 0; w < kWords; ++w) {
       const uint32_t g = (e0 >> 2) + (uint32_t)w;
