@@ -146,6 +146,45 @@ __device__ __forceinline__ void for_each_listed(const NbrCtx &c, uint32_t k, uin
   }
 }
 
+// for_each_listed with the same entries, order and calls of f, but the next
+// batch's list words are loaded into registers while the current batch's
+// neighbour data loads and computes (four more live registers per thread).
+template <int kBatch, typename Load, typename F>
+__device__ __forceinline__ void for_each_listed_ahead(const NbrCtx &c, uint32_t k,
+                                                      uint32_t cnt, Load &&load, F &&f) {
+  static_assert(kBatch % 4 == 0, "whole list words per batch");
+  constexpr int kWords = kBatch / 4;
+  uint4 cur[kWords];
+#pragma unroll
+  for (int w = 0; w < kWords; ++w)
+    cur[w] = (w == 0 || 4u * (uint32_t)w < cnt) ? load_list_word(&c.nbr4[(size_t)w * c.n + k])
+                                                : make_uint4(0u, 0u, 0u, 0u);
+  for (uint32_t e0 = 0; e0 < cnt; e0 += kBatch) {
+    uint4 nxt[kWords];
+#pragma unroll
+    for (int w = 0; w < kWords; ++w) {
+      const uint32_t g = (e0 >> 2) + (uint32_t)(kWords + w);
+      nxt[w] = 4u * g < cnt ? load_list_word(&c.nbr4[(size_t)g * c.n + k])
+                            : make_uint4(0u, 0u, 0u, 0u);
+    }
+    uint32_t slot[kBatch];
+#pragma unroll
+    for (int w = 0; w < kWords; ++w) {
+      slot[4 * w + 0] = min(cur[w].x, c.n - 1u);
+      slot[4 * w + 1] = min(cur[w].y, c.n - 1u);
+      slot[4 * w + 2] = min(cur[w].z, c.n - 1u);
+      slot[4 * w + 3] = min(cur[w].w, c.n - 1u);
+    }
+    decltype(load(0u)) data[kBatch];
+#pragma unroll
+    for (int e = 0; e < kBatch; ++e) data[e] = load(slot[e]);
+#pragma unroll
+    for (int e = 0; e < kBatch; ++e) f(data[e], e0 + (uint32_t)e < cnt);
+#pragma unroll
+    for (int w = 0; w < kWords; ++w) cur[w] = nxt[w];
+  }
+}
+
 // v' = v + dt g;  d = dt v';  p = x + d  -- rounded op by op (no
 // contraction) so that every kernel that recomputes them gets the same bits.
 __device__ __forceinline__ float4 gravity_velocity(float4 v, float dt, float gy) {
@@ -208,13 +247,20 @@ __device__ __forceinline__ void visit_fallback(const NbrCtx &c, uint32_t k, F &&
 
 // Calls f(load(slot), true) for every neighbour of particle k (and, in the
 // listed path, f(..., false) for the padding of the last group): from the
-// list when k's set fits, otherwise re-derived.
-template <int kBatch, typename Load, typename F>
+// list when k's set fits, otherwise re-derived.  kAhead selects the list
+// walk that holds the next batch's words in registers: measured faster for
+// delta-p and vorticity, slower for lambda and XSPH (whose register budgets
+// it overruns).
+template <int kBatch, bool kAhead = false, typename Load, typename F>
 __device__ __forceinline__ void visit_neighbours(const NbrCtx &c, uint32_t k, Load &&load,
                                                  F &&f) {
   const uint32_t cnt = load_own(&c.cnt[k]);
-  if (cnt <= c.maxn) for_each_listed<kBatch>(c, k, cnt, load, f);
-  else visit_fallback(c, k, [&](uint32_t j) { f(load(j), true); });
+  if (cnt <= c.maxn) {
+    if constexpr (kAhead) for_each_listed_ahead<kBatch>(c, k, cnt, load, f);
+    else for_each_listed<kBatch>(c, k, cnt, load, f);
+  } else {
+    visit_fallback(c, k, [&](uint32_t j) { f(load(j), true); });
+  }
 }
 
 __device__ __forceinline__ float ipow(float b, int e) {
@@ -489,7 +535,7 @@ __global__ void __launch_bounds__(kBlock)
   if (k >= c.n) return;
   const float4 qk = Q[k];
   float sx = 0.f, sy = 0.f, sz = 0.f;
-  visit_neighbours<kBatch>(
+  visit_neighbours<kBatch, true>(
       nc, k, [&](uint32_t j) { return __ldg(&Q[j]); },
       [&](float4 qj, bool valid) {
         const float rx = qk.x - qj.x, ry = qk.y - qj.y, rz = qk.z - qj.z;
@@ -536,7 +582,7 @@ __global__ void __launch_bounds__(kBlock)
   struct PU {
     float4 p, u;
   };
-  visit_neighbours<kBatch>(
+  visit_neighbours<kBatch, true>(
       nc, k, [&](uint32_t j) { return PU{__ldg(&P[j]), __ldg(&U[j])}; },
       [&](const PU &d, bool valid) {
     const float4 pj = d.p;
