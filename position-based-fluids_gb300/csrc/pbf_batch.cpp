@@ -232,8 +232,6 @@ int pbf_batch_create(const pbf_params *solver, uint32_t max_scenes, uint32_t max
   b->max_cells = max_cells;
   cudaError_t e = cudaGetDevice(&b->device);
   if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
-  e = paper_configure();
-  if (e != cudaSuccess) return cuda_status(e, "paper_configure");
   e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cuda_status(e, "cudaStreamCreate");
   DeviceState &d = b->d;

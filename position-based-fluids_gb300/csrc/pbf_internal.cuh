@@ -14,7 +14,6 @@ namespace pbf {
 // host reads back at synchronisation points.
 enum DeviceError : uint32_t {
   kDevErrLookback = 1u,  // a radix-sort look-back wait hit its bound
-  kDevErrStaging = 2u,   // a shared-memory staging wait hit its bound
 };
 
 // ------------------------------------------------------------ grid / scene --
@@ -222,9 +221,6 @@ cudaError_t scene_ids(const SceneDesc *scenes, uint32_t nscenes, uint32_t n, uin
 cudaError_t iota_range(uint32_t *dst, uint32_t n, cudaStream_t st);
 
 // ------------------------------------------------------- paper-mode launches
-// Raises the dynamic shared-memory limit of the gather kernels (once per
-// process and device, before the first launch).
-cudaError_t paper_configure();
 // 16-byte list words per particle for a list capacity of maxn neighbours.
 inline uint32_t paper_list_words(uint32_t maxn) { return (maxn + 3u) / 4u; }
 cudaError_t paper_predict_hash(const float4 *X, const float4 *V, uint32_t n,

@@ -734,8 +734,6 @@ NbrCtx make_ctx(const DeviceState &d, const PaperConsts &c, const uint16_t *sid)
 
 }  // namespace
 
-cudaError_t paper_configure() { return cudaSuccess; }
-
 cudaError_t paper_predict_hash(const float4 *X, const float4 *V, uint32_t n,
                                const PaperConsts &c, const SceneDesc *scenes,
                                const uint16_t *sid, uint32_t *keys,

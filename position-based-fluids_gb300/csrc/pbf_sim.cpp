@@ -291,7 +291,6 @@ int pbf_init(pbf_sim *s) {
   if (!s) return PBF_ERR_INVALID;
   if (s->inited) return PBF_ERR_STATE;
   PBF_TRY(cudaGetDevice(&s->device));
-  if (s->paper) PBF_TRY(paper_configure());
   PBF_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
   DeviceState &d = s->d;
   const size_t n = s->n;
