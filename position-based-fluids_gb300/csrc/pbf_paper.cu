@@ -286,7 +286,11 @@ __device__ __forceinline__ float scorr_term(float r2, const PaperConsts &c) {
 
 // Spiky gradient factor: grad_i W(r_vec) = f * r_vec, f = -S (h-r)^2 / r.
 __device__ __forceinline__ float spiky_factor(float r2, const PaperConsts &c) {
-  const float rinv = rsqrtf(r2);
+  // The MUFU reciprocal square root without the subnormal-input path:
+  // identical to rsqrtf for normal r^2; a subnormal r^2 (particles closer
+  // than 1e-19) is raised to the smallest normal instead of flushed to 0.
+  float rinv;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rinv) : "f"(fmaxf(r2, 1.17549435e-38f)));
   const float hr = c.h - r2 * rinv;
   return -c.spiky * hr * hr * rinv;
 }
