@@ -196,9 +196,11 @@ struct DeviceState {
   float4 *D = nullptr;                 // displacement since step start (paper)
   float4 *U = nullptr;                 // velocity and 1/rho (paper)
   float4 *W = nullptr;                 // vorticity and |omega| (paper)
-  float4 *P2 = nullptr, *DV = nullptr; // ref-compat ping-pong and dv
-  float *R = nullptr;                  // density
-  float *S = nullptr;                  // lambda (ref-compat)
+  float *R = nullptr;                  // density (paper)
+  // ref-compat: P, V and lambda by sorted slot during the step (P with the
+  // Jacobi ping-pong), and the XSPH velocity change by input index
+  float4 *PS = nullptr, *PS2 = nullptr, *VS = nullptr, *DV = nullptr;
+  float *SS = nullptr;
   uint32_t *keys = nullptr, *skeys = nullptr, *perm = nullptr;
   uint32_t *offsets = nullptr;         // ncells + 1
   uint4 *nbr = nullptr;                // neighbour lists, 4 slots per word (paper)
@@ -270,17 +272,21 @@ cudaError_t rc_predict_hash(float4 *X, float4 *V, float4 *P, uint32_t n,
                             const RefConsts &k, const SceneDesc *scenes,
                             uint32_t *keys, const SortPlan &plan,
                             uint32_t *sort_scratch, cudaStream_t st);
-cudaError_t rc_lambda(float4 *P, float *S, const uint32_t *perm,
-                      const uint32_t *offsets, uint32_t n, const RefConsts &k,
+// PS[m] = P[perm[m]]: the predicted positions by sorted slot.
+cudaError_t rc_gather(const float4 *P, const uint32_t *perm, uint32_t n, float4 *PS,
                       cudaStream_t st);
-cudaError_t rc_delta(const float4 *P, float4 *P2, const float *S,
-                     const uint32_t *perm, const uint32_t *offsets,
-                     const float4 *X, float4 *V, uint32_t n,
-                     const RefConsts &k, const SceneDesc *scenes, bool last,
-                     cudaStream_t st);
-cudaError_t rc_xsph(const float4 *P, const float4 *V, float4 *DV,
-                    const uint32_t *perm, const uint32_t *offsets, uint32_t n,
-                    const RefConsts &k, cudaStream_t st);
+// The passes read neighbours by sorted slot (PS, SS, VS) and write their own
+// slot's values there; the last delta-p pass also writes P and V by input
+// index for the commit.
+cudaError_t rc_lambda(float4 *PS, float *SS, const uint32_t *offsets, uint32_t n,
+                      const RefConsts &k, cudaStream_t st);
+cudaError_t rc_delta(const float4 *PS, float4 *PS2, const float *SS, const uint32_t *perm,
+                     const uint32_t *offsets, const float4 *X, float4 *V, float4 *P,
+                     float4 *VS, uint32_t n, const RefConsts &k, const SceneDesc *scenes,
+                     bool last, cudaStream_t st);
+cudaError_t rc_xsph(const float4 *PS, const float4 *VS, float4 *DV, const uint32_t *perm,
+                    const uint32_t *offsets, uint32_t n, const RefConsts &k,
+                    cudaStream_t st);
 cudaError_t rc_commit(float4 *X, float4 *V, const float4 *P, const float4 *DV,
                       uint32_t n, cudaStream_t st);
 

@@ -13,7 +13,10 @@
 // cell in the reference's loop order (x outer, z inner) and each cell's
 // particles in descending index -- the order a sequential launch of
 // update_cells.cl leaves in the reference's linked lists.  With that order
-// the results equal the reference's kernels bit for bit.
+// the results equal the reference's kernels bit for bit.  During the step
+// the passes keep P, V and lambda by sorted slot as well (PS, VS, SS), so a
+// cell's particles are read from consecutive slots -- the same values in
+// the same order as through the permutation.
 #include "pbf_device.cuh"
 
 namespace pbf {
@@ -22,12 +25,11 @@ namespace {
 
 constexpr int kThreads = 128;
 
-// Visits every particle j != i of the 27 cells around the current cell of
-// position p, in the reference's order.
+// Visits the sorted slot m != q of every particle of the 27 cells around the
+// current cell of position p, in the reference's order.
 template <typename F>
-__device__ __forceinline__ void ref_neighbours(uint32_t i, float4 p,
+__device__ __forceinline__ void ref_neighbours(uint32_t q, float4 p,
                                                const RefConsts &k,
-                                               const uint32_t *__restrict__ perm,
                                                const uint32_t *__restrict__ off,
                                                F &&f) {
   int cc[3];
@@ -46,9 +48,7 @@ __device__ __forceinline__ void ref_neighbours(uint32_t i, float4 p,
         const uint32_t a = __ldg(&off[ci]);
         for (uint32_t m = __ldg(&off[ci + 1]); m > a;) {
           --m;
-          // perm is a permutation of [0, n) unless the sort reported an error.
-          const uint32_t j = min(__ldg(&perm[m]), k.n - 1u);
-          if (j != i) f(j);
+          if (m != q) f(m);
         }
       }
 }
@@ -86,17 +86,24 @@ __global__ void __launch_bounds__(256)
     if (s_hist[t]) atomicAdd(&hist[t], s_hist[t]);
 }
 
+__global__ void __launch_bounds__(256)
+    k_rc_gather(const float4 *__restrict__ P, const uint32_t *__restrict__ perm, uint32_t n,
+                float4 *__restrict__ PS) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  // perm is a permutation of [0, n) unless the sort reported an error.
+  PS[q] = P[min(perm[q], n - 1u)];
+}
+
 __global__ void __launch_bounds__(kThreads)
-    k_rc_lambda(float4 *__restrict__ P, float *__restrict__ S,
-                const uint32_t *__restrict__ perm,
+    k_rc_lambda(float4 *__restrict__ PS, float *__restrict__ SS,
                 const uint32_t *__restrict__ off, uint32_t n, RefConsts k) {
   const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
-  const uint32_t i = min(perm[q], n - 1u);
-  const float4 pi = P[i];
+  const float4 pi = PS[q];
   float dens = 0.0f, gsum = 0.0f, gvx = 0.0f, gvy = 0.0f, gvz = 0.0f;
-  ref_neighbours(i, pi, k, perm, off, [&](uint32_t j) {
-    const float4 pj = P[j];
+  ref_neighbours(q, pi, k, off, [&](uint32_t m) {
+    const float4 pj = PS[m];
     const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
     if (r2 > 0.0f && r2 < k.h2) {
@@ -114,25 +121,24 @@ __global__ void __launch_bounds__(kThreads)
   });
   gsum += sqrtf(gvx * gvx + gvy * gvy + gvz * gvz);
   // Only .w changes; concurrent readers use .xyz.
-  reinterpret_cast<float *>(&P[i])[3] = dens;
+  reinterpret_cast<float *>(&PS[q])[3] = dens;
   const float c = dens / k.rest_density - 1.0f;
-  S[i] = -1.0f * c / (gsum * gsum / (k.rest_density * k.rest_density) + 10000.0f);
+  SS[q] = -1.0f * c / (gsum * gsum / (k.rest_density * k.rest_density) + 10000.0f);
 }
 
 __global__ void __launch_bounds__(kThreads)
-    k_rc_delta(const float4 *__restrict__ P, float4 *__restrict__ P2,
-               const float *__restrict__ S, const uint32_t *__restrict__ perm,
+    k_rc_delta(const float4 *__restrict__ PS, float4 *__restrict__ PS2,
+               const float *__restrict__ SS, const uint32_t *__restrict__ perm,
                const uint32_t *__restrict__ off, const float4 *__restrict__ X,
-               float4 *__restrict__ V, uint32_t n, RefConsts k,
-               const SceneDesc *__restrict__ scenes, int last) {
+               float4 *__restrict__ V, float4 *__restrict__ P, float4 *__restrict__ VS,
+               uint32_t n, RefConsts k, const SceneDesc *__restrict__ scenes, int last) {
   const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
-  const uint32_t i = min(perm[q], n - 1u);
-  const float4 pi = P[i];
-  const float si = S[i];
+  const float4 pi = PS[q];
+  const float si = SS[q];
   float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-  ref_neighbours(i, pi, k, perm, off, [&](uint32_t j) {
-    const float4 pj = P[j];
+  ref_neighbours(q, pi, k, off, [&](uint32_t m) {
+    const float4 pj = PS[m];
     const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
     if (r2 > 0.0f && r2 < k.h2) {
@@ -140,7 +146,7 @@ __global__ void __launch_bounds__(kThreads)
       const float gx = -1.0f * rx / rl * k.spiky * (k.h - rl) * (k.h - rl);
       const float gy = -1.0f * ry / rl * k.spiky * (k.h - rl) * (k.h - rl);
       const float gz = -1.0f * rz / rl * k.spiky * (k.h - rl) * (k.h - rl);
-      const float sc = si + S[j];
+      const float sc = si + SS[m];
       sx += sc * gx;
       sy += sc * gy;
       sz += sc * gz;
@@ -159,8 +165,10 @@ __global__ void __launch_bounds__(kThreads)
   // computeDelta writes delta = future - predicted; updatePredicted adds it.
   const float dx = fx - pi.x, dy = fy - pi.y, dz = fz - pi.z;
   const float4 np = make_float4(pi.x + dx, pi.y + dy, pi.z + dz, pi.w);
-  P2[i] = np;
+  PS2[q] = np;
   if (last) {
+    const uint32_t i = min(perm[q], n - 1u);
+    P[i] = np;
     // updateVelocities
     const float4 x = X[i];
     float4 v = V[i];
@@ -168,25 +176,25 @@ __global__ void __launch_bounds__(kThreads)
     v.y = (np.y - x.y) / k.dt;
     v.z = (np.z - x.z) / k.dt;
     V[i] = v;
+    VS[q] = v;
   }
 }
 
 __global__ void __launch_bounds__(kThreads)
-    k_rc_xsph(const float4 *__restrict__ P, const float4 *__restrict__ V,
+    k_rc_xsph(const float4 *__restrict__ PS, const float4 *__restrict__ VS,
               float4 *__restrict__ DV, const uint32_t *__restrict__ perm,
               const uint32_t *__restrict__ off, uint32_t n, RefConsts k) {
   const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n) return;
-  const uint32_t i = min(perm[q], n - 1u);
-  const float4 pi = P[i];
-  const float4 vi = V[i];
+  const float4 pi = PS[q];
+  const float4 vi = VS[q];
   float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-  ref_neighbours(i, pi, k, perm, off, [&](uint32_t j) {
-    const float4 pj = P[j];
+  ref_neighbours(q, pi, k, off, [&](uint32_t m) {
+    const float4 pj = PS[m];
     const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
     if (r2 > 0.0f && r2 < k.h2) {
-      const float4 vj = V[j];
+      const float4 vj = VS[m];
       const float vx = vj.x - vi.x, vy = vj.y - vi.y, vz = vj.z - vi.z;
       const float poly = k.poly6 * (k.h2 - r2) * (k.h2 - r2) * (k.h2 - r2);
       const float inv = 1.0f / pj.w;
@@ -195,7 +203,7 @@ __global__ void __launch_bounds__(kThreads)
       sz += inv * vz * poly;
     }
   });
-  DV[i] = make_float4(0.01f * sx, 0.01f * sy, 0.01f * sz, 0.0f);
+  DV[min(perm[q], n - 1u)] = make_float4(0.01f * sx, 0.01f * sy, 0.01f * sz, 0.0f);
 }
 
 __global__ void __launch_bounds__(256)
@@ -229,29 +237,31 @@ cudaError_t rc_predict_hash(float4 *X, float4 *V, float4 *P, uint32_t n,
   return cudaGetLastError();
 }
 
-cudaError_t rc_lambda(float4 *P, float *S, const uint32_t *perm,
-                      const uint32_t *offsets, uint32_t n, const RefConsts &k,
+cudaError_t rc_gather(const float4 *P, const uint32_t *perm, uint32_t n, float4 *PS,
                       cudaStream_t st) {
-  k_rc_lambda<<<blocks_for(n, kThreads), kThreads, 0, st>>>(P, S, perm, offsets,
-                                                            n, k);
+  k_rc_gather<<<blocks_for(n, 256), 256, 0, st>>>(P, perm, n, PS);
   return cudaGetLastError();
 }
 
-cudaError_t rc_delta(const float4 *P, float4 *P2, const float *S,
-                     const uint32_t *perm, const uint32_t *offsets,
-                     const float4 *X, float4 *V, uint32_t n,
-                     const RefConsts &k, const SceneDesc *scenes, bool last,
-                     cudaStream_t st) {
+cudaError_t rc_lambda(float4 *PS, float *SS, const uint32_t *offsets, uint32_t n,
+                      const RefConsts &k, cudaStream_t st) {
+  k_rc_lambda<<<blocks_for(n, kThreads), kThreads, 0, st>>>(PS, SS, offsets, n, k);
+  return cudaGetLastError();
+}
+
+cudaError_t rc_delta(const float4 *PS, float4 *PS2, const float *SS, const uint32_t *perm,
+                     const uint32_t *offsets, const float4 *X, float4 *V, float4 *P,
+                     float4 *VS, uint32_t n, const RefConsts &k, const SceneDesc *scenes,
+                     bool last, cudaStream_t st) {
   k_rc_delta<<<blocks_for(n, kThreads), kThreads, 0, st>>>(
-      P, P2, S, perm, offsets, X, V, n, k, scenes, last ? 1 : 0);
+      PS, PS2, SS, perm, offsets, X, V, P, VS, n, k, scenes, last ? 1 : 0);
   return cudaGetLastError();
 }
 
-cudaError_t rc_xsph(const float4 *P, const float4 *V, float4 *DV,
-                    const uint32_t *perm, const uint32_t *offsets, uint32_t n,
-                    const RefConsts &k, cudaStream_t st) {
-  k_rc_xsph<<<blocks_for(n, kThreads), kThreads, 0, st>>>(P, V, DV, perm,
-                                                          offsets, n, k);
+cudaError_t rc_xsph(const float4 *PS, const float4 *VS, float4 *DV, const uint32_t *perm,
+                    const uint32_t *offsets, uint32_t n, const RefConsts &k,
+                    cudaStream_t st) {
+  k_rc_xsph<<<blocks_for(n, kThreads), kThreads, 0, st>>>(PS, VS, DV, perm, offsets, n, k);
   return cudaGetLastError();
 }
 

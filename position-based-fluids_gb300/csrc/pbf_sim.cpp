@@ -174,20 +174,19 @@ int launch_step(pbf_sim *s) {
     PBF_TRY_STATUS(mark(s, 0, "sort_onesweep", 1 + passes, &ev));
     PBF_TRY(cell_offsets(d.skeys, n, s->ncells, d.offsets, st));
     PBF_TRY_STATUS(mark(s, 0, "cell_offsets", 1, &ev));
-    float4 *cur = d.P, *alt = d.P2;
+    PBF_TRY(rc_gather(d.P, d.perm, n, d.PS, st));
+    PBF_TRY_STATUS(mark(s, 0, "rc_gather", 1, &ev));
+    float4 *cur = d.PS, *alt = d.PS2;
     const uint32_t iters = s->prm.solver_iterations;
     for (uint32_t it = 0; it < iters; ++it) {
-      PBF_TRY(rc_lambda(cur, d.S, d.perm, d.offsets, n, s->rc, st));
+      PBF_TRY(rc_lambda(cur, d.SS, d.offsets, n, s->rc, st));
       PBF_TRY_STATUS(mark(s, 1, "rc_lambda", 1, &ev));
-      PBF_TRY(rc_delta(cur, alt, d.S, d.perm, d.offsets, d.X, d.V, n, s->rc,
+      PBF_TRY(rc_delta(cur, alt, d.SS, d.perm, d.offsets, d.X, d.V, d.P, d.VS, n, s->rc,
                        d.scenes, it + 1 == iters, st));
       PBF_TRY_STATUS(mark(s, 2, "rc_delta", 1, &ev));
       std::swap(cur, alt);
     }
-    if (cur != d.P)
-      PBF_TRY(cudaMemcpyAsync(d.P, cur, (size_t)n * sizeof(float4),
-                              cudaMemcpyDeviceToDevice, st));
-    PBF_TRY(rc_xsph(d.P, d.V, d.DV, d.perm, d.offsets, n, s->rc, st));
+    PBF_TRY(rc_xsph(cur, d.VS, d.DV, d.perm, d.offsets, n, s->rc, st));
     PBF_TRY_STATUS(mark(s, 3, "rc_xsph", 1, &ev));
     PBF_TRY(rc_commit(d.X, d.V, d.P, d.DV, n, st));
     PBF_TRY_STATUS(mark(s, 3, "rc_commit", 1, &ev));
@@ -323,9 +322,11 @@ int pbf_init(pbf_sim *s) {
     A(&d.nbr_cnt, n);
     A(&d.nbr, (size_t)paper_list_words(s->pc.maxn) * n);
   } else {
-    A(&d.P2, n);
+    A(&d.PS, n);
+    A(&d.PS2, n);
+    A(&d.VS, n);
     A(&d.DV, n);
-    A(&d.S, n);
+    A(&d.SS, n);
   }
   if (rc != PBF_OK) {
     free_all(s);
@@ -515,7 +516,7 @@ int pbf_launches_per_step(const pbf_sim *s, uint32_t *launches) {
     *launches = 1u /*predict+hash*/ + sort + 1u /*reorder*/ + paper_first_launches(s->d) +
                 2u * it - 1u + 2u;
   else
-    *launches = 1u + sort + 2u * it + 2u;
+    *launches = 1u + sort + 1u /*gather*/ + 2u * it + 2u;
   return PBF_OK;
 }
 
