@@ -136,7 +136,7 @@ int launch_batch_step(pbf_batch *b) {
                              st));
   PBF_TRY(sort_scan(b->plan, d.sort_scratch, st));
   PBF_TRY(sort_passes(b->plan, d.keys, nullptr, d.skeys, d.perm, d.sort_scratch, d.err, st));
-  PBF_TRY(cell_offsets(d.skeys, n, b->cells_total, d.offsets, st));
+  PBF_TRY(cell_offsets_runs(d.skeys, n, b->cells_total, d.offsets, d.runs, d.runs_count, st));
   PBF_TRY(paper_reorder(d.perm, d.X, d.V, d.ID, n, pc, d.X2, d.V2, d.ID2, d.P, d.D, st));
   const uint32_t iters = b->solver.solver_iterations;
   for (uint32_t it = 0; it < iters; ++it) {
@@ -203,7 +203,9 @@ size_t pbf_batch_device_bytes(const pbf_params *solver, uint32_t max_scenes,
   const PaperConsts pc = make_paper_consts(*solver, max_particles);
   const SortPlan plan = make_sort_plan(max_particles, 32);
   return (size_t)max_particles * bytes_per_particle(pc.maxn) +
-         ((size_t)max_cells + 1) * sizeof(uint32_t) + plan.words * sizeof(uint32_t) +
+         ((size_t)max_cells + 1) * sizeof(uint32_t) +
+         (size_t)offset_runs_capacity(max_cells) * sizeof(uint4) + sizeof(uint32_t) +
+         plan.words * sizeof(uint32_t) +
          (size_t)max_scenes * sizeof(SceneDesc) + 64;
 }
 
@@ -247,6 +249,8 @@ int pbf_batch_create(const pbf_params *solver, uint32_t max_scenes, uint32_t max
   A(&d.nbr, (size_t)paper_list_words(b->pc.maxn) * M);
   A(&d.io_pos, M); A(&d.io_vel, M);
   A(&d.offsets, (size_t)max_cells + 1);
+  A(&d.runs, offset_runs_capacity(max_cells));
+  A(&d.runs_count, 1);
   A(&d.sort_scratch, make_sort_plan(max_particles, 32).words);
   A(&d.scenes, max_scenes);
   A(&d.err, 1);
@@ -434,7 +438,7 @@ int pbf_batch_launches_per_step(const pbf_batch *b, uint32_t *launches) {
   if (!b || !launches) return PBF_ERR_INVALID;
   const SortPlan plan = make_sort_plan(std::max<uint32_t>(b->n_total, 1),
                                        bits_for(std::max<uint32_t>(b->cells_total, 1)));
-  *launches = 1u + 1u + plan.passes + 1u + 1u + paper_first_launches(b->d) +
+  *launches = 1u + 1u + plan.passes + 2u + 1u + paper_first_launches(b->d) +
               2u * b->solver.solver_iterations - 1u + 2u;
   return PBF_OK;
 }

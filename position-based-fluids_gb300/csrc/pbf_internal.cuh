@@ -101,6 +101,15 @@ cudaError_t sort_passes(const SortPlan &plan, const uint32_t *keys_in,
 cudaError_t cell_offsets(const uint32_t *sorted_keys, uint32_t n,
                          uint32_t ncells, uint32_t *offsets,
                          cudaStream_t stream);
+// The same offsets in O(n + ncells) work: every key boundary writes the run
+// of cells it starts (runs longer than 64 cells are queued in `runs`, in
+// chunks of at most 4096 cells, and filled by a second kernel).  `runs` holds
+// offset_runs_capacity(ncells) entries; *runs_count is scratch.  Two
+// kernels and one memset.
+uint32_t offset_runs_capacity(uint32_t ncells);
+cudaError_t cell_offsets_runs(const uint32_t *sorted_keys, uint32_t n, uint32_t ncells,
+                              uint32_t *offsets, uint4 *runs, uint32_t *runs_count,
+                              cudaStream_t stream);
 cudaError_t find_cells(const uint32_t *offsets, uint32_t ncells,
                        int32_t *first_last, cudaStream_t stream);
 cudaError_t cell_hash(const float4 *pred, uint32_t n, const SceneDesc &scene,
@@ -203,6 +212,8 @@ struct DeviceState {
   float *SS = nullptr;
   uint32_t *keys = nullptr, *skeys = nullptr, *perm = nullptr;
   uint32_t *offsets = nullptr;         // ncells + 1
+  uint4 *runs = nullptr;               // offset_runs_capacity(ncells) queued runs
+  uint32_t *runs_count = nullptr;
   uint4 *nbr = nullptr;                // neighbour lists, 4 slots per word (paper)
   uint32_t *nbr_cnt = nullptr;         // neighbour counts (paper)
   uint32_t *sort_scratch = nullptr;

@@ -31,6 +31,9 @@ struct pbf_sim {
   uint32_t n = 0;
   std::vector<pbf_particle> particles;
   bool paper = true;
+  // cell offsets by runs of cells (sparse grids: at least half as many
+  // cells as particles) or by one binary search per cell
+  bool offset_runs = false;
   bool inited = false;
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -122,6 +125,13 @@ int mark(pbf_sim *s, int stage, const char *name, uint32_t launches,
   return PBF_OK;
 }
 
+cudaError_t step_offsets(pbf_sim *s) {
+  DeviceState &d = s->d;
+  if (s->offset_runs)
+    return cell_offsets_runs(d.skeys, s->n, s->ncells, d.offsets, d.runs, d.runs_count, s->stream);
+  return cell_offsets(d.skeys, s->n, s->ncells, d.offsets, s->stream);
+}
+
 int launch_step(pbf_sim *s) {
   DeviceState &d = s->d;
   const cudaStream_t st = s->stream;
@@ -139,7 +149,7 @@ int launch_step(pbf_sim *s) {
     PBF_TRY(sort_passes(s->plan, d.keys, nullptr, d.skeys, d.perm,
                         d.sort_scratch, d.err, st));
     PBF_TRY_STATUS(mark(s, 0, "sort_onesweep", 1 + passes, &ev));
-    PBF_TRY(cell_offsets(d.skeys, n, s->ncells, d.offsets, st));
+    PBF_TRY(step_offsets(s));
     PBF_TRY_STATUS(mark(s, 0, "cell_offsets", 1, &ev));
     PBF_TRY(paper_reorder(d.perm, d.X, d.V, d.ID, n, s->pc, d.X2, d.V2, d.ID2,
                           d.P, d.D, st));
@@ -172,7 +182,7 @@ int launch_step(pbf_sim *s) {
     PBF_TRY(sort_passes(s->plan, d.keys, nullptr, d.skeys, d.perm,
                         d.sort_scratch, d.err, st));
     PBF_TRY_STATUS(mark(s, 0, "sort_onesweep", 1 + passes, &ev));
-    PBF_TRY(cell_offsets(d.skeys, n, s->ncells, d.offsets, st));
+    PBF_TRY(step_offsets(s));
     PBF_TRY_STATUS(mark(s, 0, "cell_offsets", 1, &ev));
     PBF_TRY(rc_gather(d.P, d.perm, n, d.PS, st));
     PBF_TRY_STATUS(mark(s, 0, "rc_gather", 1, &ev));
@@ -304,6 +314,11 @@ int pbf_init(pbf_sim *s) {
   A(&d.skeys, n);
   A(&d.perm, n);
   A(&d.offsets, (size_t)s->ncells + 1);
+  s->offset_runs = (uint64_t)s->ncells * 2u >= (uint64_t)n;
+  if (s->offset_runs) {
+    A(&d.runs, offset_runs_capacity(s->ncells));
+    A(&d.runs_count, 1);
+  }
   A(&d.sort_scratch, s->plan.words);
   A(&d.err, 1);
   A(&d.scenes, 1);
@@ -511,7 +526,7 @@ int pbf_set_graph(pbf_sim *s, int enable) {
 int pbf_launches_per_step(const pbf_sim *s, uint32_t *launches) {
   if (!s || !launches) return PBF_ERR_INVALID;
   const uint32_t it = s->prm.solver_iterations;
-  const uint32_t sort = 1u /*scan*/ + s->plan.passes + 1u /*offsets*/;
+  const uint32_t sort = 1u /*scan*/ + s->plan.passes + (s->offset_runs ? 2u : 1u) /*offsets*/;
   if (s->paper)
     *launches = 1u /*predict+hash*/ + sort + 1u /*reorder*/ + paper_first_launches(s->d) +
                 2u * it - 1u + 2u;

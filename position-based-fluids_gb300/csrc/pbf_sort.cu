@@ -249,6 +249,49 @@ __global__ void k_cell_offsets(const uint32_t *__restrict__ skeys, uint32_t n,
   off[c] = lo;
 }
 
+constexpr uint32_t kShortRun = 64;    // cells a boundary thread writes itself
+constexpr uint32_t kRunChunk = 4096;  // cells per queued chunk
+
+// One thread per key boundary i in [0, n]: the cells (key[i-1], key[i]]
+// (key[-1] = -1, key[n] = ncells) all take the value i -- the number of keys
+// below each of them.  Short runs are written here, long ones queued.
+__global__ void k_offset_runs(const uint32_t *__restrict__ skeys, uint32_t n, uint32_t ncells,
+                              uint32_t *__restrict__ off, uint4 *__restrict__ runs,
+                              uint32_t *__restrict__ runs_count, uint32_t runs_cap) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  const uint32_t lo = i == 0 ? 0u : min(skeys[i - 1], ncells - 1u) + 1u;
+  const uint32_t hi = i == n ? ncells : min(skeys[i], ncells - 1u);
+  if (hi < lo) return;
+  const uint32_t count = hi - lo + 1u;
+  if (count <= kShortRun) {
+    for (uint32_t c = lo; c <= hi; ++c) off[c] = i;
+    return;
+  }
+  const uint32_t chunks = (count + kRunChunk - 1u) / kRunChunk;
+  const uint32_t slot = atomicAdd(runs_count, chunks);
+  for (uint32_t q = 0; q < chunks; ++q) {
+    const uint32_t a = lo + q * kRunChunk;
+    const uint32_t len = min(kRunChunk, hi + 1u - a);
+    if (slot + q < runs_cap) {
+      runs[slot + q] = make_uint4(a, len, i, 0u);
+    } else {  // beyond the capacity bound (keys out of order): write it here
+      for (uint32_t c = a; c < a + len; ++c) off[c] = i;
+    }
+  }
+}
+
+// One CTA per queued chunk (grid-stride over the chunks).
+__global__ void __launch_bounds__(256)
+    k_offset_fill(const uint4 *__restrict__ runs, const uint32_t *__restrict__ runs_count,
+                  uint32_t runs_cap, uint32_t *__restrict__ off) {
+  const uint32_t total = min(*runs_count, runs_cap);
+  for (uint32_t r = blockIdx.x; r < total; r += gridDim.x) {
+    const uint4 e = runs[r];
+    for (uint32_t t = threadIdx.x; t < e.y; t += blockDim.x) off[e.x + t] = e.z;
+  }
+}
+
 __global__ void k_find_cells(const uint32_t *__restrict__ off, uint32_t ncells,
                              int2 *__restrict__ out) {
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -370,6 +413,27 @@ cudaError_t cell_offsets(const uint32_t *sorted_keys, uint32_t n,
   if (n == 0) return cudaMemsetAsync(offsets, 0, (ncells + 1ull) * 4, stream);
   k_cell_offsets<<<blocks_for(ncells + 1ull, 256), 256, 0, stream>>>(
       sorted_keys, n, ncells, offsets);
+  return cudaGetLastError();
+}
+
+uint32_t offset_runs_capacity(uint32_t ncells) {
+  // every queued run is longer than kShortRun cells and adds one chunk per
+  // kRunChunk cells or part of it
+  const uint64_t cells = (uint64_t)ncells + 1u;
+  return (uint32_t)(cells / (kShortRun + 1u) + cells / kRunChunk + 2u);
+}
+
+cudaError_t cell_offsets_runs(const uint32_t *sorted_keys, uint32_t n, uint32_t ncells,
+                              uint32_t *offsets, uint4 *runs, uint32_t *runs_count,
+                              cudaStream_t stream) {
+  const uint32_t cap = offset_runs_capacity(ncells);
+  cudaError_t e = cudaMemsetAsync(runs_count, 0, sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return e;
+  k_offset_runs<<<blocks_for(n + 1ull, 256), 256, 0, stream>>>(sorted_keys, n, ncells, offsets,
+                                                               runs, runs_count, cap);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_offset_fill<<<min(cap, kStrideCtas / 2u), 256, 0, stream>>>(runs, runs_count, cap, offsets);
   return cudaGetLastError();
 }
 

@@ -141,3 +141,25 @@ def test_hash_ref_compat_grid_matches_reference_lists(pbf, golden, oracle_mod):
                          torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()
         assert np.array_equal(dh.cpu().numpy().view(np.uint32), golden[f"{name}/k1/cell"]), name
+
+
+@pytest.mark.parametrize("mode", ["paper", "ref_compat"])
+def test_step_cell_ranges_on_a_sparse_grid(pbf, oracle_mod, mode):
+    """The step's cell offsets (every key boundary writes the run of cells it
+    starts; runs over 64 cells are queued in chunks of at most 4096 and filled
+    by a second kernel) against the inclusive ranges of the sorted keys: a
+    small block in the corner of a 16 x 16 x 64-cell box leaves empty runs of
+    thousands of cells."""
+    m = pbf.MODE_PAPER if mode == "paper" else pbf.MODE_REF_COMPAT
+    p = pbf.scenes.base_params((1.6, 1.6, 6.4), (16, 16, 64), mode=m)
+    ps = pbf.scenes.block((0.1, 0.1, 0.1), (10, 6, 12), seed=44)
+    with pbf.Simulation(p, ps) as sim:
+        sim.init()
+        sim.step(2)
+        hsh, _, rng = sim.cells()
+    nc = p.ncells
+    sk = np.sort(hsh)
+    assert np.array_equal(rng, oracle_mod.find_cells(sk, nc))
+    empty = rng[:, 0] < 0
+    runs = np.diff(np.flatnonzero(np.diff(np.r_[0, empty.astype(np.int8), 0]) != 0))[::2]
+    assert runs.max() > 4096  # the queued, chunked path ran
