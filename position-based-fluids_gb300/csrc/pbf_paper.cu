@@ -37,7 +37,10 @@
 // once) are loaded without allocating in L1 and first in line for eviction
 // from L2, and the values a thread reads only for itself skip L1 as well, so
 // both caches keep the neighbour data that dozens of threads re-read (7%
-// off the whole step on GB300).
+// off the whole step on GB300).  The next batch's list words are prefetched
+// into L2 (lambda, XSPH) or loaded into registers one batch ahead (delta-p,
+// vorticity, whose register budgets allow it), so a batch's neighbour loads
+// do not wait on a list word from DRAM.
 //
 // Measured on GB300 (1M-particle dam break after 500 steps, per step):
 // absolute 32-bit entries run 9% faster than 16-bit entries relative to a
