@@ -1,6 +1,6 @@
 """The full-size workloads (1,048,576 and 4,194,304 particles, paper
-equations), where the FP64 oracle is too slow to run, through properties that
-do not depend on size:
+equations), where running the FP64 oracle over many steps is too slow,
+through properties that do not depend on size:
 
   * two runs from the same state give the same bits (fixed summation order);
   * the scene run inside a batch gives the same bits as the plain simulation
@@ -8,15 +8,20 @@ do not depend on size:
   * neighbour lists capped at 16 entries -- most particles then re-derive
     their sets from the cells in every pass -- give the same bits as the
     default capacity (same members, same order, same arithmetic);
-  * every position stays finite and inside the walls.
+  * every position stays finite and inside the walls;
 
-The per-step error against the FP64 oracle is checked on the 32,768-particle
-configuration of the same dam break (test_gpu_paper.py).
+and one step of the 1M scene, from its initial block and from its state
+after 12 steps, against the FP64 oracle on all host cores (<= 1e-5 h in
+position; the measured error is printed as a JSON line).
 """
 from __future__ import annotations
 
+import json
+
 import numpy as np
 import pytest
+
+import __graft_entry__ as ge
 
 pytestmark = pytest.mark.gpu
 
@@ -66,3 +71,28 @@ def test_double_dam_break_4m(pbf):
     again = run(pbf, sc.params, sc.particles, 6)
     for x, y in zip(again, ref):
         assert np.array_equal(bits(x), bits(y))
+
+
+def test_single_scene_1m_step_vs_fp64_oracle(pbf, oracle_mod):
+    sc = pbf.scenes.config_1m()
+    h = sc.params.h
+    with pbf.Simulation(sc.params, sc.particles) as sim:
+        sim.init()
+        sim.step(STEPS)
+        moving = sim.dumpData()
+    prm = ge.paper_params_for_oracle(sc.params)
+    for label, (pos, vel) in (("initial block", pbf.state_from_particles(sc.particles)),
+                              (f"step {STEPS}", moving)):
+        with pbf.Simulation(sc.params, sc.particles) as sim:
+            sim.init()
+            sim.set_state(pos, vel)
+            sim.step(1)
+            gp, gv = sim.dumpData()
+        op, ov, *_ = oracle_mod.paper_steps_f64(prm, pos.astype(np.float64), vel.astype(np.float64), 1)
+        perr = np.abs(gp[:, :3].astype(np.float64) - op[:, :3]).max()
+        vmax = np.abs(ov[:, :3]).max()
+        verr = np.abs(gv[:, :3].astype(np.float64) - ov[:, :3]).max()
+        print(json.dumps({"fp64_step_error": {"scene": sc.name, "particles": sc.n, "from": label,
+                                              "pos_max_h": perr / h, "vel_max": verr, "vmax": vmax}}))
+        assert perr <= 1e-5 * h, f"position error {perr / h:.3e} h"
+        assert verr <= 1e-3 + 1e-4 * vmax, f"velocity error {verr}"
