@@ -128,3 +128,25 @@ def test_single_scene_1m_density_over_500_steps(pbf):
     assert inside_walls(sc.params, pos)
     assert worst[0] <= 0.35 and worst[1] <= 4.5 and worst[2] <= 0.35
     assert late <= 0.02
+
+
+def test_double_dam_break_4m_step_vs_fp64_oracle(pbf, oracle_mod):
+    """One step of the 4.2M double dam break, from its state after 6 steps,
+    against the FP64 oracle on all host cores (<= 1e-5 h in position)."""
+    sc = pbf.scenes.config_4m()
+    h = sc.params.h
+    pos, vel = run(pbf, sc.params, sc.particles, 6)
+    with pbf.Simulation(sc.params, sc.particles) as sim:
+        sim.init()
+        sim.set_state(pos, vel)
+        sim.step(1)
+        gp, gv = sim.dumpData()
+    prm = ge.paper_params_for_oracle(sc.params)
+    op, ov, *_ = oracle_mod.paper_steps_f64(prm, pos.astype(np.float64), vel.astype(np.float64), 1)
+    perr = np.abs(gp[:, :3].astype(np.float64) - op[:, :3]).max()
+    vmax = np.abs(ov[:, :3]).max()
+    verr = np.abs(gv[:, :3].astype(np.float64) - ov[:, :3]).max()
+    print(json.dumps({"fp64_step_error": {"scene": sc.name, "particles": sc.n, "from": "step 6",
+                                          "pos_max_h": perr / h, "vel_max": verr, "vmax": vmax}}))
+    assert perr <= 1e-5 * h, f"position error {perr / h:.3e} h"
+    assert verr <= 1e-3 + 1e-4 * vmax, f"velocity error {verr}"
