@@ -10,9 +10,12 @@ through properties that do not depend on size:
     default capacity (same members, same order, same arithmetic);
   * every position stays finite and inside the walls;
 
-and one step of the 1M scene, from its initial block and from its state
-after 12 steps, against the FP64 oracle on all host cores (<= 1e-5 h in
-position; the measured error is printed as a JSON line).
+and one step of the 1M scene (from its initial block and from its state
+after 12 steps) and of the 4.2M scene against the FP64 oracle on all host
+cores (<= 1e-5 h in position; the measured error is printed as a JSON
+line), the 1M scene's density error over its 500 steps, and two steps of
+the 1M scene in REF_COMPAT mode bit for bit against the reference's own
+kernels.
 """
 from __future__ import annotations
 
@@ -150,3 +153,28 @@ def test_double_dam_break_4m_step_vs_fp64_oracle(pbf, oracle_mod):
                                           "pos_max_h": perr / h, "vel_max": verr, "vmax": vmax}}))
     assert perr <= 1e-5 * h, f"position error {perr / h:.3e} h"
     assert verr <= 1e-3 + 1e-4 * vmax, f"velocity error {verr}"
+
+
+def test_single_scene_1m_ref_compat_matches_reference_kernels(pbf, oracle_mod):
+    """REF_COMPAT at the headline size: two steps of the 1M scene in the
+    reference's equations, bit for bit against the reference's own kernels
+    (compiled from their .cl sources; cell lists built by a sequential
+    update_cells launch, as the GPU path visits them) on all host cores."""
+    if not oracle_mod.reference_available():
+        pytest.skip("the reference's kernels are not built on this host")
+    sc = pbf.scenes.config_1m()
+    p = sc.params.copy()
+    p.mode = pbf.MODE_REF_COMPAT
+    cfg = oracle_mod.Config(p.x_min, p.x_max, p.y_min, p.y_max, p.z_min, p.z_max, p.x_n, p.y_n,
+                            p.z_n, p.time_step_length, p.rest_density)
+    pos0, vel0 = pbf.state_from_particles(sc.particles)
+    rp, rv, rpred, *_ = oracle_mod.reference_steps(cfg, pos0, vel0, 2)
+    with pbf.Simulation(p, sc.particles) as sim:
+        sim.init()
+        sim.initCells()
+        sim.step(2)
+        gp, gv = sim.dumpData()
+        gd = sim.density()
+    assert np.array_equal(bits(gp), bits(rp))
+    assert np.array_equal(bits(gv), bits(rv))
+    assert np.array_equal(bits(gd), bits(rpred[:, 3]))
