@@ -178,3 +178,27 @@ def test_single_scene_1m_ref_compat_matches_reference_kernels(pbf, oracle_mod):
     assert np.array_equal(bits(gp), bits(rp))
     assert np.array_equal(bits(gv), bits(rv))
     assert np.array_equal(bits(gd), bits(rpred[:, 3]))
+
+
+def test_benchmark_mix_alone_vs_mix(pbf):
+    """The 256-scene batched benchmark mix (14.6M particles, N log-uniform
+    4,096-262,144) for 5 steps: eight scenes across the size range, each run
+    alone in a batch of one, give the same bits as in the mix."""
+    scenes = pbf.scenes.mixed_batch(256)
+    solver = scenes[0].params
+    n_tot = sum(s.n for s in scenes)
+    cells = sum(s.params.ncells for s in scenes)
+    pick = np.argsort([s.n for s in scenes])[np.linspace(0, len(scenes) - 1, 8).astype(int)]
+    with pbf.Batch(solver, len(scenes), n_tot, cells) as bt:
+        ids = [bt.add_scene(s.params, s.particles) for s in scenes]
+        bt.step(5)
+        mixed = {int(i): bt.dump_scene(ids[i]) for i in pick}
+    for i in pick:
+        s = scenes[int(i)]
+        with pbf.Batch(solver, 1, s.n, s.params.ncells) as one:
+            sid = one.add_scene(s.params, s.particles)
+            one.step(5)
+            alone = one.dump_scene(sid)
+        assert inside_walls(s.params, alone[0])
+        for x, y in zip(alone, mixed[int(i)]):
+            assert np.array_equal(bits(x), bits(y)), s.name
