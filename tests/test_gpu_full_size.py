@@ -202,3 +202,32 @@ def test_benchmark_mix_alone_vs_mix(pbf):
         assert inside_walls(s.params, alone[0])
         for x, y in zip(alone, mixed[int(i)]):
             assert np.array_equal(bits(x), bits(y)), s.name
+
+
+def test_served_stream_alone_vs_mix(pbf):
+    """The first 24 requests of the served benchmark stream (N log-uniform
+    8,192-524,288, 100-1000 steps) submitted two per turn of the request
+    loop under a 16 GB budget: four requests across the size range give the
+    same bits as their scene stepped alone in a batch of one."""
+    reqs = pbf.scenes.request_stream(1.0)[:24]
+    scenes = [r.scene() for r in reqs]
+    solver = scenes[0].params
+    pick = [int(i) for i in np.argsort([r.n for r in reqs])[np.linspace(0, len(reqs) - 1, 4).astype(int)]]
+    with pbf.Server(solver, 16 << 30, max_scenes=64, cells_per_particle=2.0, max_chunk=64) as srv:
+        rids = []
+        for k in range(0, len(reqs), 2):
+            for r, s in zip(reqs[k:k + 2], scenes[k:k + 2]):
+                rids.append(srv.submit(s.params, s.particles, r.steps))
+            srv.poll(wait=True)
+        srv.run_until_idle()
+        assert srv.stats()["completed"] == len(reqs)
+        results = {i: srv.result(rids[i]) for i in pick}
+    for i in pick:
+        r, s = reqs[i], scenes[i]
+        with pbf.Batch(solver, 1, s.n, s.params.ncells) as one:
+            sid = one.add_scene(s.params, s.particles)
+            one.step(r.steps)
+            want = one.dump_scene(sid)
+        assert inside_walls(s.params, want[0])
+        for x, y in zip(results[i], want):
+            assert np.array_equal(bits(x), bits(y)), f"request {r.index} ({s.n} particles, {r.steps} steps)"
