@@ -68,19 +68,26 @@ struct pbf_server {
 namespace {
 
 // Retires finished requests: final state to host, scene out of the batch.
+// On an error the failing request and every one after it stay active, so
+// the active list always matches the scenes in the batch.
 int retire(pbf_server *s, std::vector<uint64_t> &done) {
   std::vector<uint64_t> keep;
   keep.reserve(s->active.size());
+  int rc = PBF_OK;
   for (uint64_t id : s->active) {
     Request &r = s->reqs[id];
-    if (r.steps_done < r.steps) {
+    if (rc != PBF_OK || r.steps_done < r.steps) {
       keep.push_back(id);
       continue;
     }
     r.pos.assign((size_t)r.n * 4, 0.0f);
     r.vel.assign((size_t)r.n * 4, 0.0f);
-    PBF_TRY_STATUS(pbf_batch_dump_scene(s->batch, r.scene, r.pos.data(), r.vel.data()));
-    PBF_TRY_STATUS(pbf_batch_remove_scene(s->batch, r.scene));
+    rc = pbf_batch_dump_scene(s->batch, r.scene, r.pos.data(), r.vel.data());
+    if (rc == PBF_OK) rc = pbf_batch_remove_scene(s->batch, r.scene);
+    if (rc != PBF_OK) {
+      keep.push_back(id);
+      continue;
+    }
     r.state = PBF_REQ_DONE;
     s->active_particles -= r.n;
     s->active_cells -= r.cells;
@@ -88,7 +95,7 @@ int retire(pbf_server *s, std::vector<uint64_t> &done) {
     done.push_back(id);
   }
   s->active.swap(keep);
-  return PBF_OK;
+  return rc;
 }
 
 // Admits queued requests, first fit in arrival order.
