@@ -19,6 +19,9 @@ Our arm prints one JSON line with:
   roofline  the dominant kernel's algorithmic bytes per launch over its
             average launch time (a second timed pass with an event after
             every launch), against the measured HBM copy bandwidth;
+  density_error  the density constraint's error in the final state
+            (mean and max compression, interior mean |rho/rho0 - 1|), read
+            back after the timed region;
   cpu_baseline  the reference's own kernels (compiled from their sources)
             or, where they are absent, the oracle's restatement of them, on a
             bounded sample of the same workload on the host cores.
@@ -89,6 +92,19 @@ def measured_peaks() -> dict:
         d = json.loads(p.read_text())
         return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
     return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def density_error_of(sim, rest_density: float, at_step: int) -> dict:
+    """The density constraint's error in the state just stepped (from its
+    last lambda pass, read back after the timed region): mean and max
+    compression max(rho/rho0 - 1, 0), and mean |rho/rho0 - 1| over particles
+    away from the free surface (rho >= 0.8 rho0)."""
+    rho = sim.density() / rest_density
+    comp = np.maximum(rho - 1.0, 0.0)
+    interior = rho >= 0.8
+    return {"at_step": at_step, "mean_compression": float(comp.mean()),
+            "max_compression": float(comp.max()),
+            "mean_abs_interior": float(np.abs(rho[interior] - 1.0).mean()) if interior.any() else 0.0}
 
 
 def profile_traffic(kernel: str):
@@ -318,6 +334,7 @@ def run_ours(args) -> int:
     clock_summary = clocks.summary()
     if args.save_state and rank == 0:
         sim.save_state(args.save_state)
+    density_error = density_error_of(sim, sc.params.rest_density, args.warmup + args.steps)
 
     # ---- end to end through the C-ABI with host buffers ------------------
     nbytes = n * 16
@@ -406,6 +423,7 @@ def run_ours(args) -> int:
                          "velocity": float(stages[3])},
             "kernel_ms_per_step": {k: v[0] / kt_steps for k, v in kt.items()},
             "clocks": clock_summary,
+            "density_error": density_error,
             "cpu_baseline": cpu,
             "ref_equations": ref_eq,
         }
