@@ -698,6 +698,81 @@ def form_summaries(args) -> dict:
     return out
 
 
+def run_aux(args) -> int:
+    """The rows around the step, on the 1M-particle scene: scenario files
+    (write and read, text .in and binary; host), the headless runner's
+    per-step time with no snapshots, binary VTK snapshots and text .in
+    snapshots every 10 steps (pbf_run, 120 steps, the snapshots copied into
+    page-locked buffers and written by host threads while stepping goes
+    on), and one 1280 x 720 point-sprite frame (device time plus read-back;
+    median of 7)."""
+    import re
+
+    import torch
+
+    import __graft_entry__ as ge
+
+    world, rank, local = dist_info()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    pbf = ge.load_package()
+    sc = pbf.scenes.config_1m()
+    out = {"metric": "aux", "workload": "aux_1m", "particles": sc.n}
+    with tempfile.TemporaryDirectory() as d:
+        d = Path(d)
+        io = {}
+        for kind, binary in (("text", False), ("binary", True)):
+            f = d / f"scene_{kind}.in"
+            t0 = time.perf_counter()
+            pbf.write_particles(f, sc.particles, binary=binary)
+            t1 = time.perf_counter()
+            back = pbf.read_particles(f)
+            t2 = time.perf_counter()
+            assert np.array_equal(back["x"], sc.particles["x"])
+            io[kind] = {"write_s": t1 - t0, "read_s": t2 - t1, "bytes": f.stat().st_size}
+        out["scenario_io"] = io
+        runner = {}
+        for label, part_freq, vtk_freq in (("no snapshots", 0, 0), ("vtk every 10 steps", 0, 10),
+                                           (".in every 10 steps", 10, 0)):
+            p = sc.params.copy()
+            p.part_input_file = b"scene_binary.in"
+            p.time_end = np.float32(120.5 * p.time_step_length)
+            p.part_out_freq = part_freq
+            p.part_out_name_base = str(d / "snap_").encode()
+            p.vtk_out_freq = vtk_freq
+            p.vtk_out_name_base = str(d / "frame_").encode()
+            pbf.write_config(d / "scene.par", p)
+            t0 = time.perf_counter()
+            r = subprocess.run([str(pbf.PKG_DIR / "pbf_run"), str(d / "scene.par")],
+                               capture_output=True, text=True, timeout=600)
+            wall = time.perf_counter() - t0
+            if r.returncode != 0:
+                raise RuntimeError(r.stderr)
+            mean = float(re.search(r"mean:\s*([0-9.eE+-]+)", r.stdout).group(1))
+            runner[label] = {"mean_step_s": mean, "wall_s": wall,
+                             "files": len(list(d.glob("snap_*"))) + len(list(d.glob("frame_*")))}
+            for f in [*d.glob("snap_*"), *d.glob("frame_*")]:
+                f.unlink()
+        base = runner["no snapshots"]["mean_step_s"]
+        for v in runner.values():
+            v["vs_no_snapshots"] = v["mean_step_s"] / base
+        out["runner"] = runner
+    with pbf.Simulation(sc.params, sc.particles) as sim:
+        sim.init()
+        sim.step(10)
+        sim.render(width=1280, height=720)
+        times = []
+        for _ in range(7):
+            t0 = time.perf_counter()
+            img = sim.render(width=1280, height=720)
+            times.append(time.perf_counter() - t0)
+    out["render"] = {"width": 1280, "height": 720, "median_ms": statistics.median(times) * 1e3,
+                     "lit_fraction": float((img.max(axis=2) > 0).mean())}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -705,9 +780,11 @@ def main() -> int:
                     help="timed steps (default 500 for the single scene, 300 for the batch)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["single", "large", "batch", "serve"], default="single",
+    ap.add_argument("--workload", choices=["single", "large", "batch", "serve", "aux"],
+                    default="single",
                     help="single: the 1M-particle scene (headline); large: the 4.2M-particle double "
-                         "dam break; batch; serve")
+                         "dam break; batch; serve; aux: scenario I/O, runner snapshots and "
+                         "rendering around the 1M step")
     ap.add_argument("--serve-seconds", type=float, default=6.0, help="arrival window of the served stream")
     ap.add_argument("--hbm-budget-gb", type=float, default=120.0, help="HBM budget of the request loop")
     ap.add_argument("--max-chunk", type=int, default=16, help="most batched steps per loop turn")
@@ -735,6 +812,8 @@ def main() -> int:
         return run_batch(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "aux":
+        return run_aux(args)
     return run_ours(args)
 
 
