@@ -43,6 +43,9 @@ solves, N log-uniform 8,192..524,288, 100..1000 steps each, submitted in
 real time for --serve-seconds to the request loop (continuous batching
 under a 120 GB HBM budget); p50/p99 completion latency; against the same
 requests solved one at a time on the plain path.
+--workload aux: the rows around the step on the 1M scene (scenario file
+I/O text vs binary, the headless runner's snapshot cost, a 1280 x 720
+render), printed as one line with "metric": "aux".
 --save-state / --load-state write and resume the single scene's state (for
 profiling a late state of the simulation).
 
