@@ -1,8 +1,9 @@
 """Edge cases of the paper-mode step on the GPU against the FP64 oracle:
 a single particle, particles started outside the box or on cell faces, a
 fluid packed into one cell (every particle over the list capacity, so every
-pass re-derives the set), a grid of one cell along an axis, and batches that
-are emptied and refilled.
+pass re-derives the set), a grid of one cell along an axis, batches that
+are emptied and refilled, solver iteration counts other than 4, and cells
+longer than h.
 
 Tolerance: positions within 1e-5 h of the oracle after one step from the
 same state (the PAPER-mode bound), or bitwise where the statement is about
@@ -117,3 +118,38 @@ def test_batch_emptied_and_refilled(pbf):
             want = sim.dumpData()
         for x, y in zip(got, want):
             assert np.array_equal(bits(x), bits(y))
+
+
+@pytest.mark.parametrize("iterations", [1, 2, 7])
+def test_solver_iteration_counts(pbf, oracle_mod, iterations):
+    """The step with other solver iteration counts (the lists are built
+    before the first lambda and read by every iteration) against the FP64
+    oracle, from a moving state."""
+    sc = pbf.scenes.dam_break((12, 12, 12), (0.8, 0.8, 1.6), seed=71)
+    p = sc.params.copy()
+    p.solver_iterations = iterations
+    with pbf.Simulation(p, sc.particles) as sim:
+        sim.init()
+        sim.step(20)
+        pos, vel = sim.dumpData()
+    with pbf.Simulation(p, sc.particles) as sim:
+        sim.init()
+        sim.set_state(pos, vel)
+        sim.step(1)
+        gp, _ = sim.dumpData()
+    op, *_ = oracle_mod.paper_steps_f64(ge.paper_params_for_oracle(p),
+                                        pos.astype(np.float64), vel.astype(np.float64), 1)
+    err = np.abs(gp[:, :3].astype(np.float64) - op[:, :3]).max()
+    assert err <= POS_TOL_H * p.h, f"{err / p.h:.3e} h"
+
+
+def test_cells_longer_than_h(pbf, oracle_mod):
+    """Cells 1.5 h long along y (the 27 cells then reach past h; members are
+    still exactly the particles within h) against the FP64 oracle."""
+    p = pbf.scenes.base_params((0.8, 1.2, 0.8), (8, 8, 8))
+    ps = pbf.scenes.block((0.05, 0.05, 0.05), (10, 14, 10), seed=72)
+    with pbf.Simulation(p, ps) as sim:
+        sim.init()
+        sim.step(10)
+        pos, vel = sim.dumpData()
+    one_step_vs_oracle(pbf, oracle_mod, p, pbf.particles_from_state(pos, vel))
