@@ -370,30 +370,24 @@ __global__ void __launch_bounds__(256)
   D[k] = make_float4(d.x, d.y, d.z, 0.0f);
 }
 
-// Neighbour-list build over the 27 cells from the predicted positions P
-// (which equal the step-start positions the fallback recomputes).  Each
-// member's slot is stored straight into its list word; entries past the
-// count in the last word are left as they are (readers mask them).  The
-// self pair and coincident particles drop out through r^2 > 0.
-template <int kBlock>
-__global__ void __launch_bounds__(kBlock)
-    k_nbr_build(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
-                uint4 *__restrict__ nbr4, uint32_t *__restrict__ nbr_cnt) {
-  const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
-  if (k >= c.n) return;
-  const SceneDesc &s = scene_of(nc.scenes, nc.sid, k);
-  const float4 pk = P[k];
+// Calls member(j, rx, ry, rz, r2) for every slot j with 0 < r2 = |p_k - p_j|^2
+// < h^2 in the 27 cells around k's cell (key `key`), in the order the lists
+// store and the re-derived path visits: rows by (dz, dy), each row's slots
+// ascending.  The self pair and coincident particles drop out through
+// r^2 > 0.
+template <typename F>
+__device__ __forceinline__ void scan_members(const float4 &pk, uint32_t key, const SceneDesc &s,
+                                             const uint32_t *__restrict__ off,
+                                             const float4 *__restrict__ P, const PaperConsts &c,
+                                             F &&member) {
   const int nx = s.ncell[0], ny = s.ncell[1], nz = s.ncell[2];
-  const uint32_t local = nc.skeys[k] - s.cell_base;
+  const uint32_t local = key - s.cell_base;
   const int cx = (int)(local % (uint32_t)nx);
   const uint32_t t = local / (uint32_t)nx;
   const int cy = (int)(t % (uint32_t)ny);
   const int cz = (int)(t / (uint32_t)ny);
   const int x0 = cx > 0 ? cx - 1 : 0;
   const int x1 = cx + 1 < nx ? cx + 1 : nx - 1;
-  uint32_t *__restrict__ out = reinterpret_cast<uint32_t *>(nbr4) + 4ull * k;
-  const size_t stride = 4ull * c.n;  // words from one list group to the next
-  uint32_t cnt = 0;
   for (int dz = -1; dz <= 1; ++dz) {
     const int z = cz + dz;
     if (z < 0 || z >= nz) continue;
@@ -401,8 +395,8 @@ __global__ void __launch_bounds__(kBlock)
       const int y = cy + dy;
       if (y < 0 || y >= ny) continue;
       const uint32_t row = s.cell_base + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
-      const uint32_t a = __ldg(&nc.off[row + x0]);
-      const uint32_t b = __ldg(&nc.off[row + x1 + 1]);
+      const uint32_t a = __ldg(&off[row + x0]);
+      const uint32_t b = __ldg(&off[row + x1 + 1]);
       // whole groups of four candidates (loads at fixed offsets from one
       // pointer, no per-load bound), then the last one to three
       uint32_t j = a;
@@ -415,10 +409,7 @@ __global__ void __launch_bounds__(kBlock)
         for (int e = 0; e < 4; ++e) {
           const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
           const float r2 = rx * rx + ry * ry + rz * rz;
-          if (r2 > 0.0f && r2 < c.h2) {
-            if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j + e;
-            ++cnt;
-          }
+          if (r2 > 0.0f && r2 < c.h2) member(j + e, rx, ry, rz, r2);
         }
       }
       if (j < b) {
@@ -429,14 +420,32 @@ __global__ void __launch_bounds__(kBlock)
         for (int e = 0; e < 3; ++e) {
           const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
           const float r2 = rx * rx + ry * ry + rz * rz;
-          if (j + e < b && r2 > 0.0f && r2 < c.h2) {
-            if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j + e;
-            ++cnt;
-          }
+          if (j + e < b && r2 > 0.0f && r2 < c.h2) member(j + e, rx, ry, rz, r2);
         }
       }
     }
   }
+}
+
+// Neighbour-list build from the predicted positions P (which equal the
+// step-start positions the fallback recomputes).  Each member's slot is
+// stored straight into its list word; entries past the count in the last
+// word are left as they are (readers mask them).
+template <int kBlock>
+__global__ void __launch_bounds__(kBlock)
+    k_nbr_build(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
+                uint4 *__restrict__ nbr4, uint32_t *__restrict__ nbr_cnt) {
+  const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
+  if (k >= c.n) return;
+  const float4 pk = P[k];
+  uint32_t *__restrict__ out = reinterpret_cast<uint32_t *>(nbr4) + 4ull * k;
+  const size_t stride = 4ull * c.n;  // words from one list group to the next
+  uint32_t cnt = 0;
+  scan_members(pk, nc.skeys[k], scene_of(nc.scenes, nc.sid, k), nc.off, P, c,
+               [&](uint32_t j, float, float, float, float) {
+                 if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j;
+                 ++cnt;
+               });
   nbr_cnt[k] = cnt;
 }
 
@@ -452,63 +461,17 @@ __global__ void __launch_bounds__(kBlock)
                  float4 *__restrict__ Q, float *__restrict__ R) {
   const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
   if (k >= c.n) return;
-  const SceneDesc &s = scene_of(nc.scenes, nc.sid, k);
   const float4 pk = P[k];
-  const int nx = s.ncell[0], ny = s.ncell[1], nz = s.ncell[2];
-  const uint32_t local = nc.skeys[k] - s.cell_base;
-  const int cx = (int)(local % (uint32_t)nx);
-  const uint32_t t = local / (uint32_t)nx;
-  const int cy = (int)(t % (uint32_t)ny);
-  const int cz = (int)(t / (uint32_t)ny);
-  const int x0 = cx > 0 ? cx - 1 : 0;
-  const int x1 = cx + 1 < nx ? cx + 1 : nx - 1;
   uint32_t *__restrict__ out = reinterpret_cast<uint32_t *>(nbr4) + 4ull * k;
   const size_t stride = 4ull * c.n;  // words from one list group to the next
   uint32_t cnt = 0;
   LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
-  for (int dz = -1; dz <= 1; ++dz) {
-    const int z = cz + dz;
-    if (z < 0 || z >= nz) continue;
-    for (int dy = -1; dy <= 1; ++dy) {
-      const int y = cy + dy;
-      if (y < 0 || y >= ny) continue;
-      const uint32_t row = s.cell_base + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
-      const uint32_t a = __ldg(&nc.off[row + x0]);
-      const uint32_t b = __ldg(&nc.off[row + x1 + 1]);
-      uint32_t j = a;
-      for (; j + 4u <= b; j += 4) {
-        const float4 *__restrict__ q = P + j;
-        float4 d[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) d[e] = __ldg(q + e);
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
-          const float r2 = rx * rx + ry * ry + rz * rz;
-          if (r2 > 0.0f && r2 < c.h2) {
-            if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j + e;
-            ++cnt;
-            acc.add(rx, ry, rz, r2, c);
-          }
-        }
-      }
-      if (j < b) {
-        float4 d[3];
-#pragma unroll
-        for (int e = 0; e < 3; ++e) d[e] = __ldg(&P[min(j + e, b - 1u)]);
-#pragma unroll
-        for (int e = 0; e < 3; ++e) {
-          const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
-          const float r2 = rx * rx + ry * ry + rz * rz;
-          if (j + e < b && r2 > 0.0f && r2 < c.h2) {
-            if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j + e;
-            ++cnt;
-            acc.add(rx, ry, rz, r2, c);
-          }
-        }
-      }
-    }
-  }
+  scan_members(pk, nc.skeys[k], scene_of(nc.scenes, nc.sid, k), nc.off, P, c,
+               [&](uint32_t j, float rx, float ry, float rz, float r2) {
+                 if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j;
+                 ++cnt;
+                 acc.add(rx, ry, rz, r2, c);
+               });
   nbr_cnt[k] = cnt;
   Q[k] = make_float4(pk.x, pk.y, pk.z, acc.lambda(c));
   R[k] = acc.rho;
