@@ -262,3 +262,48 @@ def test_selftest_argument_checks(pbf):
     assert pbf.lib().pbf_selftest_bounded_wait(0, C.byref(flag)) == pbf.ERR_INVALID
     assert pbf.lib().pbf_selftest_bounded_wait(1 << 27, C.byref(flag)) == pbf.ERR_INVALID
     assert pbf.lib().pbf_selftest_bounded_wait(100, None) == pbf.ERR_INVALID
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include <string.h>
+#include "pbf.h"
+
+/* every entry point pbf.h declares, referenced so the linker resolves each */
+static void *const entry_points[] = {
+%s
+};
+
+int main(void) {
+  pbf_params p;
+  pbf_params_default(&p);
+  if (pbf_abi_version() != 1) return 1;
+  if (strcmp(pbf_status_string(PBF_ERR_INVALID), "invalid argument") != 0) return 2;
+  printf("abi %%d entry points %%zu h %%g\n", pbf_abi_version(),
+         sizeof entry_points / sizeof entry_points[0], (double)((p.x_max - p.x_min) / p.x_n));
+  return 0;
+}
+"""
+
+
+def test_header_is_c_and_every_entry_point_links(pbf, tmp_path):
+    """A C11 caller (gcc -Wall -Wextra -Werror) includes pbf.h, takes the
+    address of every function it declares, links against the library and
+    runs its host-only entry points -- the boundary as a C program sees it."""
+    import shutil
+    import subprocess
+
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    names = declared_functions()
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER % ",\n".join(f"    (void *){n}" for n in names))
+    exe = tmp_path / "caller"
+    lib_dir = pbf.LIB_PATH.parent
+    cmd = ["gcc", "-std=c11", "-Wall", "-Wextra", "-Werror", "-Wno-pedantic", f"-I{ROOT / 'include'}",
+           str(src), f"-L{lib_dir}", f"-l:{pbf.LIB_PATH.name}", f"-Wl,-rpath,{lib_dir}", "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr
+    assert f"entry points {len(names)}" in out.stdout and "h 0.1" in out.stdout
