@@ -1,8 +1,8 @@
 """CPU oracle for the position-based-fluids step -- TEST INFRASTRUCTURE.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
-leg import this package, and only as the checker (or the timed CPU
-baseline).  The product library never links or calls it.
+leg import this package, and only as the oracle results are compared
+against (or the timed CPU baseline).  The product library never links or calls it.
 
 Two native libraries back it (``oracle/build.py`` builds both):
 
@@ -10,7 +10,7 @@ Two native libraries back it (``oracle/build.py`` builds both):
   restated (REF_COMPAT, float and double), the PBF_PAPER equations in double,
   and the sort-path intent (hash, stable sort, inclusive cell ranges);
 * ``reference`` -- the reference's own ``src/kernels/*.cl`` compiled as C++
-  (``oracle/ref_driver.cpp``); present only where the reference tree, or its
+  (``oracle/ref_launch.cpp``); present only where the reference tree, or its
   preprocessed kernel text in ``oracle/_ref``, was available at build time.
 """
 from __future__ import annotations

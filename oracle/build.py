@@ -6,7 +6,7 @@ Two libraries come out of it:
   (``oracle/pbf_oracle.cpp``), built from this repository's own sources.
 * ``oracle/_ref/libpbfref.so`` -- the reference's own live kernels
   (MrMagne/position-based-fluids ``src/kernels/*.cl``) compiled as C++ through
-  ``oracle/clshim.hpp`` and driven by ``oracle/ref_driver.cpp``.
+  ``oracle/clshim.hpp`` and launched by ``oracle/ref_launch.cpp``.
 
 The reference sources are read where they lie, under ``/root/reference``; they
 are never copied into the repository.  The first stage runs the C++
@@ -103,8 +103,8 @@ def build_reference(force: bool = False) -> Path | None:
     units = [REF_DIR / f"{k}.pre.cl" for k in LIVE_KERNELS]
     if not all(u.exists() for u in units):
         return None
-    driver = ORACLE_DIR / "ref_driver.cpp"
-    deps = units + [driver, ORACLE_DIR / "clshim.hpp", ORACLE_DIR / "clshim_predict.hpp"]
+    launcher = ORACLE_DIR / "ref_launch.cpp"
+    deps = units + [launcher, ORACLE_DIR / "clshim.hpp", ORACLE_DIR / "clshim_predict.hpp"]
     if not (force or _stale(REFERENCE_LIB, deps)):
         return REFERENCE_LIB
     objs = []
@@ -113,8 +113,8 @@ def build_reference(force: bool = False) -> Path | None:
         o = REF_DIR / f"{k}.o"
         objs.append(o)
         jobs.append([CXX, *COMMON, "-w", "-x", "c++", "-include", str(_shim_for(k)), "-c", str(u), "-o", str(o)])
-    dobj = REF_DIR / "ref_driver.o"
-    jobs.append([CXX, *COMMON, "-c", str(driver), "-o", str(dobj)])
+    dobj = REF_DIR / "ref_launch.o"
+    jobs.append([CXX, *COMMON, "-c", str(launcher), "-o", str(dobj)])
     with ThreadPoolExecutor(max_workers=8) as ex:
         list(ex.map(_run, jobs))
     _run([CXX, *COMMON, "-shared", *map(str, objs), str(dobj), "-o", str(REFERENCE_LIB)])

@@ -9,14 +9,14 @@
  *
  * What is rendered here, and the semantics chosen where OpenCL leaves room:
  *   - address-space qualifiers (__kernel/__global/__local) vanish;
- *   - get_global_id(0) reads a thread-local work-item id that the driver
- *     (oracle/ref_driver.cpp) sets before each call, one call per work-item;
+ *   - get_global_id(0) reads a thread-local work-item id that the launcher
+ *     (oracle/ref_launch.cpp) sets before each call, one call per work-item;
  *   - float3 / float4 with component access (.x .y .z .w), the .xyz swizzle
  *     (read, write, +=), and the element-wise operators the kernels use;
  *   - length(v) = sqrt((x*x + y*y) + z*z), evaluated in that order;
  *   - atomic_xchg on int via the GCC builtin;
  *   - the -D constants that src/main.cpp:149-168 bakes into the program are
- *     routed to a global struct (clshim_k) that the driver fills with the
+ *     routed to a global struct (clshim_k) that the launcher fills with the
  *     same 6-significant-digit values main.cpp prints.
  *
  * All arithmetic is IEEE-754 binary32 with FMA contraction disabled

@@ -1,14 +1,15 @@
 /*
  * TEST INFRASTRUCTURE (oracle) -- never linked into the product library.
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
- * it, and only as a checker or as the timed CPU baseline.
+ * it, and only as the oracle results are compared against or as the timed
+ * CPU baseline.
  *
  * CPU restatement of the position-based-fluids step of the reference
  * (MrMagne/position-based-fluids).  See pbf_oracle.h for the C-ABI.
  *
  * Pinning: the float instantiation of the REF_COMPAT step is checked, bit for
  * bit, against the reference's own kernels compiled from their .cl sources
- * (oracle/ref_driver.cpp), on the reference's scenario files.
+ * (oracle/ref_launch.cpp), on the reference's scenario files.
  */
 #include "pbf_oracle.h"
 

@@ -1,7 +1,8 @@
 /*
  * TEST INFRASTRUCTURE (oracle) -- never linked into the product library.
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
- * the library built from these declarations, and only as a checker.
+ * the library built from these declarations, and only as the oracle results
+ * are compared against.
  *
  * C-ABI of the CPU restatement in oracle/pbf_oracle.cpp:
  *   - REF_COMPAT step: the reference's live kernels restated line by line

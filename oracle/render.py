@@ -1,5 +1,5 @@
 """Test infrastructure: a numpy restatement of the reference's particle
-drawing, the checker for the CUDA renderer (pbf_render).
+drawing, the oracle for the CUDA renderer (pbf_render).
 
 Follows src/visual/visual.cpp (camera sphere :86-100, look-at :104-125,
 perspective and box centring :217-227, clear colour and depth test

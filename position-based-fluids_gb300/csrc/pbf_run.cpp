@@ -1,4 +1,4 @@
-// Headless driver: the reference's main() (src/main.cpp:40-189) without the
+// Headless runner: the reference's main() (src/main.cpp:40-189) without the
 // window, the OpenCL setup or the renderer.
 //
 //   pbf_run <scenario.par> [--root DIR] [--waves] [--out positions.txt]

@@ -2,7 +2,7 @@
 
 Source of truth: the reference's own live kernels (MrMagne/position-based-
 fluids src/kernels/*.cl) compiled as C++ by oracle/build.py and run by
-oracle/ref_driver.cpp, in the step order of src/Simulation.cpp:455-576,
+oracle/ref_launch.cpp, in the step order of src/Simulation.cpp:455-576,
 with update_cells.cl launched in ascending work-item order.  Inputs are the
 reference's scenario files (assets/scenarios/*.par + *.in), read here and
 stored in the fixture so that the tests need neither the reference tree nor

@@ -236,7 +236,7 @@ def test_ppm_writer(pbf, tmp_path):
 
 
 def test_render_restatement_single_particle(pbf):
-    """The renderer's checker: one particle at the box centre seen by the
+    """The renderer's oracle: one particle at the box centre seen by the
     reference's initial camera is a disc at the image centre, (|v|, |v|, 1)
     at its middle (normal towards the camera), on the 0.05 grey background."""
     from oracle import render as oracle_render
