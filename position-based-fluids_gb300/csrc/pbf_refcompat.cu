@@ -25,13 +25,16 @@ namespace {
 
 constexpr int kThreads = 128;
 
-// Visits the sorted slot m != q of every particle of the 27 cells around the
-// current cell of position p, in the reference's order.
-template <typename F>
+// Calls f(m, load(m)) for the sorted slot m != q of every particle of the 27
+// cells around the current cell of position p, in the reference's order.
+// A cell's slots are loaded kGroup at a time (indices clamped into the cell),
+// so the group's loads are in flight together; f still sees them one by one
+// in descending slot order.
+template <int kGroup = 4, typename Load, typename F>
 __device__ __forceinline__ void ref_neighbours(uint32_t q, float4 p,
                                                const RefConsts &k,
                                                const uint32_t *__restrict__ off,
-                                               F &&f) {
+                                               Load &&load, F &&f) {
   int cc[3];
   cc[0] = (int)((p.x - k.min[0]) / k.clen[0]);
   cc[1] = (int)((p.y - k.min[1]) / k.clen[1]);
@@ -46,9 +49,15 @@ __device__ __forceinline__ void ref_neighbours(uint32_t q, float4 p,
           continue;
         const uint32_t ci = (uint32_t)n0 + (uint32_t)nx * ((uint32_t)n1 + (uint32_t)ny * (uint32_t)n2);
         const uint32_t a = __ldg(&off[ci]);
-        for (uint32_t m = __ldg(&off[ci + 1]); m > a;) {
-          --m;
-          if (m != q) f(m);
+        for (uint32_t top = __ldg(&off[ci + 1]); top > a; top = top - a > kGroup ? top - kGroup : a) {
+          decltype(load(0u)) d[kGroup];
+#pragma unroll
+          for (int e = 0; e < kGroup; ++e) d[e] = load(top - a > (uint32_t)e ? top - 1u - e : a);
+#pragma unroll
+          for (int e = 0; e < kGroup; ++e) {
+            const uint32_t m = top - 1u - e;
+            if (top - a > (uint32_t)e && m != q) f(m, d[e]);
+          }
         }
       }
 }
@@ -102,8 +111,7 @@ __global__ void __launch_bounds__(kThreads)
   if (q >= n) return;
   const float4 pi = PS[q];
   float dens = 0.0f, gsum = 0.0f, gvx = 0.0f, gvy = 0.0f, gvz = 0.0f;
-  ref_neighbours(q, pi, k, off, [&](uint32_t m) {
-    const float4 pj = PS[m];
+  ref_neighbours(q, pi, k, off, [&](uint32_t m) { return PS[m]; }, [&](uint32_t, float4 pj) {
     const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
     if (r2 > 0.0f && r2 < k.h2) {
@@ -137,8 +145,14 @@ __global__ void __launch_bounds__(kThreads)
   const float4 pi = PS[q];
   const float si = SS[q];
   float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-  ref_neighbours(q, pi, k, off, [&](uint32_t m) {
-    const float4 pj = PS[m];
+  struct PSl {
+    float4 p;
+    float s;
+  };
+  ref_neighbours(
+      q, pi, k, off, [&](uint32_t m) { return PSl{__ldg(&PS[m]), __ldg(&SS[m])}; },
+      [&](uint32_t, const PSl &d) {
+    const float4 pj = d.p;
     const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
     if (r2 > 0.0f && r2 < k.h2) {
@@ -146,7 +160,7 @@ __global__ void __launch_bounds__(kThreads)
       const float gx = -1.0f * rx / rl * k.spiky * (k.h - rl) * (k.h - rl);
       const float gy = -1.0f * ry / rl * k.spiky * (k.h - rl) * (k.h - rl);
       const float gz = -1.0f * rz / rl * k.spiky * (k.h - rl) * (k.h - rl);
-      const float sc = si + SS[m];
+      const float sc = si + d.s;
       sx += sc * gx;
       sy += sc * gy;
       sz += sc * gz;
@@ -189,12 +203,11 @@ __global__ void __launch_bounds__(kThreads)
   const float4 pi = PS[q];
   const float4 vi = VS[q];
   float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-  ref_neighbours(q, pi, k, off, [&](uint32_t m) {
-    const float4 pj = PS[m];
+  ref_neighbours(q, pi, k, off, [&](uint32_t m) { return __ldg(&PS[m]); }, [&](uint32_t m, float4 pj) {
     const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
     if (r2 > 0.0f && r2 < k.h2) {
-      const float4 vj = VS[m];
+      const float4 vj = __ldg(&VS[m]);
       const float vx = vj.x - vi.x, vy = vj.y - vi.y, vz = vj.z - vi.z;
       const float poly = k.poly6 * (k.h2 - r2) * (k.h2 - r2) * (k.h2 - r2);
       const float inv = 1.0f / pj.w;
