@@ -115,9 +115,11 @@ __device__ __forceinline__ float load_own(const float *p) {
 
 // For the `cnt` listed neighbours of particle k, kBatch (4 or 8) at a time:
 // the batch's list words, then load(slot) for every entry of the batch, then
-// f(data, valid) for each in list order -- the loads of a batch are in
-// flight together.  Slots are clamped to the arrays (entries past the count
-// in the last word are whatever an earlier step left there).
+// f(data) for each in list order -- the loads of a batch are in flight
+// together.  The list build pads the last word with k's own slot and words
+// past the count read as k: those entries are the particle itself, which
+// every pass drops through r^2 > 0, so no entry needs a bound or a count
+// test.
 template <int kBatch, typename Load, typename F>
 __device__ __forceinline__ void for_each_listed(const NbrCtx &c, uint32_t k, uint32_t cnt,
                                                 Load &&load, F &&f) {
@@ -135,17 +137,17 @@ __device__ __forceinline__ void for_each_listed(const NbrCtx &c, uint32_t k, uin
     for (int w = 0; w < kWords; ++w) {
       const uint32_t g = (e0 >> 2) + (uint32_t)w;
       const uint4 v = (w == 0 || 4u * g < cnt) ? load_list_word(&c.nbr4[(size_t)g * c.n + k])
-                                                : make_uint4(0u, 0u, 0u, 0u);
-      slot[4 * w + 0] = min(v.x, c.n - 1u);
-      slot[4 * w + 1] = min(v.y, c.n - 1u);
-      slot[4 * w + 2] = min(v.z, c.n - 1u);
-      slot[4 * w + 3] = min(v.w, c.n - 1u);
+                                                : make_uint4(k, k, k, k);
+      slot[4 * w + 0] = v.x;
+      slot[4 * w + 1] = v.y;
+      slot[4 * w + 2] = v.z;
+      slot[4 * w + 3] = v.w;
     }
     decltype(load(0u)) data[kBatch];
 #pragma unroll
     for (int e = 0; e < kBatch; ++e) data[e] = load(slot[e]);
 #pragma unroll
-    for (int e = 0; e < kBatch; ++e) f(data[e], e0 + (uint32_t)e < cnt);
+    for (int e = 0; e < kBatch; ++e) f(data[e]);
   }
 }
 
@@ -161,28 +163,28 @@ __device__ __forceinline__ void for_each_listed_ahead(const NbrCtx &c, uint32_t 
 #pragma unroll
   for (int w = 0; w < kWords; ++w)
     cur[w] = (w == 0 || 4u * (uint32_t)w < cnt) ? load_list_word(&c.nbr4[(size_t)w * c.n + k])
-                                                : make_uint4(0u, 0u, 0u, 0u);
+                                                : make_uint4(k, k, k, k);
   for (uint32_t e0 = 0; e0 < cnt; e0 += kBatch) {
     uint4 nxt[kWords];
 #pragma unroll
     for (int w = 0; w < kWords; ++w) {
       const uint32_t g = (e0 >> 2) + (uint32_t)(kWords + w);
       nxt[w] = 4u * g < cnt ? load_list_word(&c.nbr4[(size_t)g * c.n + k])
-                            : make_uint4(0u, 0u, 0u, 0u);
+                            : make_uint4(k, k, k, k);
     }
     uint32_t slot[kBatch];
 #pragma unroll
     for (int w = 0; w < kWords; ++w) {
-      slot[4 * w + 0] = min(cur[w].x, c.n - 1u);
-      slot[4 * w + 1] = min(cur[w].y, c.n - 1u);
-      slot[4 * w + 2] = min(cur[w].z, c.n - 1u);
-      slot[4 * w + 3] = min(cur[w].w, c.n - 1u);
+      slot[4 * w + 0] = cur[w].x;
+      slot[4 * w + 1] = cur[w].y;
+      slot[4 * w + 2] = cur[w].z;
+      slot[4 * w + 3] = cur[w].w;
     }
     decltype(load(0u)) data[kBatch];
 #pragma unroll
     for (int e = 0; e < kBatch; ++e) data[e] = load(slot[e]);
 #pragma unroll
-    for (int e = 0; e < kBatch; ++e) f(data[e], e0 + (uint32_t)e < cnt);
+    for (int e = 0; e < kBatch; ++e) f(data[e]);
 #pragma unroll
     for (int w = 0; w < kWords; ++w) cur[w] = nxt[w];
   }
@@ -248,9 +250,9 @@ __device__ __forceinline__ void visit_fallback(const NbrCtx &c, uint32_t k, F &&
   });
 }
 
-// Calls f(load(slot), true) for every neighbour of particle k (and, in the
-// listed path, f(..., false) for the padding of the last group): from the
-// list when k's set fits, otherwise re-derived.  kAhead selects the list
+// Calls f(load(slot)) for every neighbour of particle k (and, in the listed
+// path, for k itself as the padding of the last group): from the list when
+// k's set fits, otherwise re-derived.  kAhead selects the list
 // walk that holds the next batch's words in registers: measured faster for
 // delta-p and vorticity, slower for lambda and XSPH (whose register budgets
 // it overruns).
@@ -262,7 +264,7 @@ __device__ __forceinline__ void visit_neighbours(const NbrCtx &c, uint32_t k, Lo
     if constexpr (kAhead) for_each_listed_ahead<kBatch>(c, k, cnt, load, f);
     else for_each_listed<kBatch>(c, k, cnt, load, f);
   } else {
-    visit_fallback(c, k, [&](uint32_t j) { f(load(j), true); });
+    visit_fallback(c, k, [&](uint32_t j) { f(load(j)); });
   }
 }
 
@@ -427,10 +429,18 @@ __device__ __forceinline__ void scan_members(const float4 &pk, uint32_t key, con
   }
 }
 
+// Fills the rest of a listed set's last word with the particle's own slot
+// (maxn is a multiple of 8, so the word is inside the list capacity).
+__device__ __forceinline__ void pad_list(uint32_t *__restrict__ out, size_t stride,
+                                         uint32_t cnt, uint32_t maxn, uint32_t k) {
+  if (cnt <= maxn)
+    for (uint32_t e = cnt; e & 3u; ++e) out[(size_t)(e >> 2) * stride + (e & 3u)] = k;
+}
+
 // Neighbour-list build from the predicted positions P (which equal the
 // step-start positions the fallback recomputes).  Each member's slot is
-// stored straight into its list word; entries past the count in the last
-// word are left as they are (readers mask them).
+// stored straight into its list word; the rest of the last word holds the
+// particle's own slot.
 template <int kBlock>
 __global__ void __launch_bounds__(kBlock)
     k_nbr_build(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
@@ -446,6 +456,7 @@ __global__ void __launch_bounds__(kBlock)
                  if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j;
                  ++cnt;
                });
+  pad_list(out, stride, cnt, c.maxn, k);
   nbr_cnt[k] = cnt;
 }
 
@@ -472,6 +483,7 @@ __global__ void __launch_bounds__(kBlock)
                  ++cnt;
                  acc.add(rx, ry, rz, r2, c);
                });
+  pad_list(out, stride, cnt, c.maxn, k);
   nbr_cnt[k] = cnt;
   Q[k] = make_float4(pk.x, pk.y, pk.z, acc.lambda(c));
   R[k] = acc.rho;
@@ -487,10 +499,10 @@ __global__ void __launch_bounds__(kBlock)
   LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
   visit_neighbours<kBatch>(
       nc, k, [&](uint32_t j) { return __ldg(&P[j]); },
-      [&](float4 pj, bool valid) {
+      [&](float4 pj) {
         const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
         const float r2 = rx * rx + ry * ry + rz * rz;
-        if (valid && r2 > 0.0f && r2 < c.h2) acc.add(rx, ry, rz, r2, c);
+        if (r2 > 0.0f && r2 < c.h2) acc.add(rx, ry, rz, r2, c);
       });
   Q[k] = make_float4(pk.x, pk.y, pk.z, acc.lambda(c));
   R[k] = acc.rho;
@@ -507,10 +519,10 @@ __global__ void __launch_bounds__(kBlock)
   float sx = 0.f, sy = 0.f, sz = 0.f;
   visit_neighbours<kBatch, true>(
       nc, k, [&](uint32_t j) { return __ldg(&Q[j]); },
-      [&](float4 qj, bool valid) {
+      [&](float4 qj) {
         const float rx = qk.x - qj.x, ry = qk.y - qj.y, rz = qk.z - qj.z;
         const float r2 = rx * rx + ry * ry + rz * rz;
-        if (valid && r2 > 0.0f && r2 < c.h2) {
+        if (r2 > 0.0f && r2 < c.h2) {
           const float wgt = (qk.w + qj.w + scorr_term(r2, c)) * spiky_factor(r2, c);
           sx += wgt * rx;
           sy += wgt * ry;
@@ -554,11 +566,11 @@ __global__ void __launch_bounds__(kBlock)
   };
   visit_neighbours<kBatch, true>(
       nc, k, [&](uint32_t j) { return PU{__ldg(&P[j]), __ldg(&U[j])}; },
-      [&](const PU &d, bool valid) {
+      [&](const PU &d) {
     const float4 pj = d.p;
     const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
-    if (valid && r2 > 0.0f && r2 < c.h2) {
+    if (r2 > 0.0f && r2 < c.h2) {
       const float4 uj = d.u;
       const float f = spiky_factor(r2, c) * uj.w;
       const float gx = f * rx, gy = f * ry, gz = f * rz;
@@ -573,11 +585,12 @@ __global__ void __launch_bounds__(kBlock)
   PW[k] = make_float4(pk.x, pk.y, pk.z, wn);
 }
 
-// At least 1152 resident threads per SM: 56 registers (64 at 256 threads),
-// no spills in any shape; left to itself the compiler takes 63 (96 with
-// eight loads in flight) and halves the resident warps.
+// At least 1152 resident threads per SM with four loads in flight (56
+// registers; 64 at 256 threads), 1024 with eight (64 registers): no spills
+// in any shape.  Left to itself the compiler takes 63 (96 with eight loads
+// in flight) and halves the resident warps.
 template <int kBlock, int kBatch>
-__global__ void __launch_bounds__(kBlock, 1152 / kBlock)
+__global__ void __launch_bounds__(kBlock, (kBatch == 8 ? 1024 : 1152) / kBlock)
     k_xsph_commit(const float4 *__restrict__ PW, const float4 *__restrict__ U,
                   const float4 *__restrict__ Wv, NbrCtx nc, PaperConsts c,
                   const uint32_t *__restrict__ ID2, float4 *__restrict__ X,
@@ -593,11 +606,11 @@ __global__ void __launch_bounds__(kBlock, 1152 / kBlock)
   };
   visit_neighbours<kBatch>(
       nc, k, [&](uint32_t j) { return PU{__ldg(&PW[j]), __ldg(&U[j])}; },
-      [&](const PU &d, bool valid) {
+      [&](const PU &d) {
     const float4 pj = d.p;
     const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
-    if (valid && r2 > 0.0f && r2 < c.h2) {
+    if (r2 > 0.0f && r2 < c.h2) {
       const float4 uj = d.u;
       const float e = spiky_factor(r2, c) * uj.w * (pj.w - wk.w);
       ex += e * rx;
