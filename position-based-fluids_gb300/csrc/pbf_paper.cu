@@ -20,9 +20,10 @@
 //   U       (velocity, 1/rho) as read by the velocity passes
 //   W       (vorticity, |vorticity|)
 // Neighbour sets are built once per step from the predicted positions
-// (Algorithm 1 line 6): N_k = { j != k : 0 < |p_k - p_j| < h } over the 27
-// cells around k's cell.  Every later pass evaluates the kernels at the
-// current positions with W = 0 beyond h.
+// (Algorithm 1 line 6): N_k = { j != k : r0 <= |p_k - p_j| < h } over the
+// 27 cells around k's cell, r0 = sqrt(FLT_MIN) ~ 1.1e-19 (closer particles
+// count as coincident).  Every later pass evaluates the kernels at the
+// current positions with W = 0 beyond h and below r0.
 //
 // Gather passes run one thread per sorted particle.  Neighbour lists hold
 // each neighbour as its 32-bit sorted slot, four per 16-byte word: group g of
@@ -118,8 +119,8 @@ __device__ __forceinline__ float load_own(const float *p) {
 // f(data) for each in list order -- the loads of a batch are in flight
 // together.  The list build pads the last word with k's own slot and words
 // past the count read as k: those entries are the particle itself, which
-// every pass drops through r^2 > 0, so no entry needs a bound or a count
-// test.
+// every pass drops through the pair test (r^2 = 0), so no entry needs a
+// bound or a count test.
 template <int kBatch, typename Load, typename F>
 __device__ __forceinline__ void for_each_listed(const NbrCtx &c, uint32_t k, uint32_t cnt,
                                                 Load &&load, F &&f) {
@@ -208,6 +209,13 @@ __device__ __forceinline__ float3 start_position(const NbrCtx &c, uint32_t j) {
   return add3(__ldg(&c.X2[j]), displacement(__ldg(&c.V2[j]), c.dt));
 }
 
+// Particles j != k closer than h form a pair.  Distances below
+// sqrt(FLT_MIN) ~ 1.1e-19 count as coincident (like r = 0, whose direction
+// is undefined), so r^2 is a normal number wherever a kernel is evaluated.
+__device__ __forceinline__ bool is_pair(float r2, float h2) {
+  return r2 >= 1.17549435e-38f && r2 < h2;
+}
+
 // Visits the 9 rows around the cell with key `key` (order: dz, dy, slot);
 // f(q, j) gets the row index q = (dz+1)*3 + (dy+1) and the slot j != k.
 template <typename F>
@@ -246,7 +254,7 @@ __device__ __forceinline__ void visit_fallback(const NbrCtx &c, uint32_t k, F &&
     const float3 pj = start_position(c, j);
     const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
-    if (r2 > 0.0f && r2 < c.h2) f(j);
+    if (is_pair(r2, c.h2)) f(j);
   });
 }
 
@@ -289,13 +297,12 @@ __device__ __forceinline__ float scorr_term(float r2, const PaperConsts &c) {
   return -c.scorr_k * ipow(ratio, c.scorr_n3);
 }
 
-// Spiky gradient factor: grad_i W(r_vec) = f * r_vec, f = -S (h-r)^2 / r.
+// Spiky gradient factor: grad_i W(r_vec) = f * r_vec, f = -S (h-r)^2 / r,
+// for a pair (r^2 normal, so the MUFU reciprocal square root without the
+// subnormal-input path equals rsqrtf).
 __device__ __forceinline__ float spiky_factor(float r2, const PaperConsts &c) {
-  // The MUFU reciprocal square root without the subnormal-input path:
-  // identical to rsqrtf for normal r^2; a subnormal r^2 (particles closer
-  // than 1e-19) is raised to the smallest normal instead of flushed to 0.
   float rinv;
-  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rinv) : "f"(fmaxf(r2, 1.17549435e-38f)));
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rinv) : "f"(r2));
   const float hr = c.h - r2 * rinv;
   return -c.spiky * hr * hr * rinv;
 }
@@ -372,11 +379,11 @@ __global__ void __launch_bounds__(256)
   D[k] = make_float4(d.x, d.y, d.z, 0.0f);
 }
 
-// Calls member(j, rx, ry, rz, r2) for every slot j with 0 < r2 = |p_k - p_j|^2
-// < h^2 in the 27 cells around k's cell (key `key`), in the order the lists
-// store and the re-derived path visits: rows by (dz, dy), each row's slots
-// ascending.  The self pair and coincident particles drop out through
-// r^2 > 0.
+// Calls member(j, rx, ry, rz, r2) for every slot j that forms a pair with k
+// (is_pair(r2 = |p_k - p_j|^2)) in the 27 cells around k's cell (key `key`),
+// in the order the lists store and the re-derived path visits: rows by
+// (dz, dy), each row's slots ascending.  The self pair and coincident
+// particles drop out.
 template <typename F>
 __device__ __forceinline__ void scan_members(const float4 &pk, uint32_t key, const SceneDesc &s,
                                              const uint32_t *__restrict__ off,
@@ -411,7 +418,7 @@ __device__ __forceinline__ void scan_members(const float4 &pk, uint32_t key, con
         for (int e = 0; e < 4; ++e) {
           const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
           const float r2 = rx * rx + ry * ry + rz * rz;
-          if (r2 > 0.0f && r2 < c.h2) member(j + e, rx, ry, rz, r2);
+          if (is_pair(r2, c.h2)) member(j + e, rx, ry, rz, r2);
         }
       }
       if (j < b) {
@@ -422,7 +429,7 @@ __device__ __forceinline__ void scan_members(const float4 &pk, uint32_t key, con
         for (int e = 0; e < 3; ++e) {
           const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
           const float r2 = rx * rx + ry * ry + rz * rz;
-          if (j + e < b && r2 > 0.0f && r2 < c.h2) member(j + e, rx, ry, rz, r2);
+          if (j + e < b && is_pair(r2, c.h2)) member(j + e, rx, ry, rz, r2);
         }
       }
     }
@@ -502,7 +509,7 @@ __global__ void __launch_bounds__(kBlock)
       [&](float4 pj) {
         const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
         const float r2 = rx * rx + ry * ry + rz * rz;
-        if (r2 > 0.0f && r2 < c.h2) acc.add(rx, ry, rz, r2, c);
+        if (is_pair(r2, c.h2)) acc.add(rx, ry, rz, r2, c);
       });
   Q[k] = make_float4(pk.x, pk.y, pk.z, acc.lambda(c));
   R[k] = acc.rho;
@@ -522,7 +529,7 @@ __global__ void __launch_bounds__(kBlock)
       [&](float4 qj) {
         const float rx = qk.x - qj.x, ry = qk.y - qj.y, rz = qk.z - qj.z;
         const float r2 = rx * rx + ry * ry + rz * rz;
-        if (r2 > 0.0f && r2 < c.h2) {
+        if (is_pair(r2, c.h2)) {
           const float wgt = (qk.w + qj.w + scorr_term(r2, c)) * spiky_factor(r2, c);
           sx += wgt * rx;
           sy += wgt * ry;
@@ -570,7 +577,7 @@ __global__ void __launch_bounds__(kBlock)
     const float4 pj = d.p;
     const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
-    if (r2 > 0.0f && r2 < c.h2) {
+    if (is_pair(r2, c.h2)) {
       const float4 uj = d.u;
       const float f = spiky_factor(r2, c) * uj.w;
       const float gx = f * rx, gy = f * ry, gz = f * rz;
@@ -610,7 +617,7 @@ __global__ void __launch_bounds__(kBlock, (kBatch == 8 ? 1024 : 1152) / kBlock)
     const float4 pj = d.p;
     const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
     const float r2 = rx * rx + ry * ry + rz * rz;
-    if (r2 > 0.0f && r2 < c.h2) {
+    if (is_pair(r2, c.h2)) {
       const float4 uj = d.u;
       const float e = spiky_factor(r2, c) * uj.w * (pj.w - wk.w);
       ex += e * rx;
