@@ -53,6 +53,8 @@
 // raised the L1 hit rate from 69% to 77% but ran 4% slower; four threads per
 // particle (neighbour entries split between them, shuffle reduction) ran
 // 1.4x slower.
+#include <type_traits>
+
 #include "pbf_device.cuh"
 
 namespace pbf {
@@ -286,15 +288,18 @@ __device__ __forceinline__ float ipow(float b, int e) {
   return r;
 }
 
-// -k h^2 (W(r)/W(dq h))^n with W(r)/W(dq h) = ((h^2-r^2)/(h^2-dq^2 h^2))^3.
+// -k h^2 (W(r)/W(dq h))^n with W(r)/W(dq h) = ((h^2-r^2)/(h^2-dq^2 h^2))^3;
+// kTwelve: the exponent 3n is 12 (n = 4, the paper's choice).
+template <bool kTwelve>
 __device__ __forceinline__ float scorr_term(float r2, const PaperConsts &c) {
   const float ratio = (c.h2 - r2) * c.inv_scorr_den;
-  if (c.scorr_n3 == 12) {
+  if constexpr (kTwelve) {
     const float r3 = ratio * ratio * ratio;
     const float r6 = r3 * r3;
     return -c.scorr_k * (r6 * r6);
+  } else {
+    return -c.scorr_k * ipow(ratio, c.scorr_n3);
   }
-  return -c.scorr_k * ipow(ratio, c.scorr_n3);
 }
 
 // Spiky gradient factor: grad_i W(r_vec) = f * r_vec, f = -S (h-r)^2 / r,
@@ -524,18 +529,24 @@ __global__ void __launch_bounds__(kBlock)
   if (k >= c.n) return;
   const float4 qk = Q[k];
   float sx = 0.f, sy = 0.f, sz = 0.f;
-  visit_neighbours<kBatch, true>(
-      nc, k, [&](uint32_t j) { return __ldg(&Q[j]); },
-      [&](float4 qj) {
-        const float rx = qk.x - qj.x, ry = qk.y - qj.y, rz = qk.z - qj.z;
-        const float r2 = rx * rx + ry * ry + rz * rz;
-        if (is_pair(r2, c.h2)) {
-          const float wgt = (qk.w + qj.w + scorr_term(r2, c)) * spiky_factor(r2, c);
-          sx += wgt * rx;
-          sy += wgt * ry;
-          sz += wgt * rz;
-        }
-      });
+  // one neighbour walk per s_corr exponent form, chosen once per thread
+  const auto walk = [&](auto twelve) {
+    visit_neighbours<kBatch, true>(
+        nc, k, [&](uint32_t j) { return __ldg(&Q[j]); },
+        [&](float4 qj) {
+          const float rx = qk.x - qj.x, ry = qk.y - qj.y, rz = qk.z - qj.z;
+          const float r2 = rx * rx + ry * ry + rz * rz;
+          if (is_pair(r2, c.h2)) {
+            const float wgt = (qk.w + qj.w + scorr_term<decltype(twelve)::value>(r2, c)) *
+                              spiky_factor(r2, c);
+            sx += wgt * rx;
+            sy += wgt * ry;
+            sz += wgt * rz;
+          }
+        });
+  };
+  if (c.scorr_n3 == 12) walk(std::true_type{});
+  else walk(std::false_type{});
   const float4 x = load_own(&nc.X2[k]);
   const float4 d0 = load_own(&D[k]);
   float3 d = make_float3(d0.x + sx * c.inv_rho0, d0.y + sy * c.inv_rho0,
