@@ -83,11 +83,14 @@ __device__ __forceinline__ const SceneDesc &scene_of(const SceneDesc *scenes,
 }
 
 // List words are read once per pass: load them without keeping them in L1
-// and first in line for eviction from L2, so the caches keep the neighbour
-// data that is re-read.
-__device__ __forceinline__ uint4 load_list_word(const uint4 *p) {
+// and first in line for eviction from L2 (policy from l2_evict_first), so
+// the caches keep the neighbour data that is re-read.
+__device__ __forceinline__ uint64_t l2_evict_first() {
   uint64_t policy;
   asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(policy));
+  return policy;
+}
+__device__ __forceinline__ uint4 load_list_word(const uint4 *p, uint64_t policy) {
   uint4 v;
   asm volatile(
       "ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
@@ -128,6 +131,7 @@ __device__ __forceinline__ void for_each_listed(const NbrCtx &c, uint32_t k, uin
                                                 Load &&load, F &&f) {
   static_assert(kBatch % 4 == 0, "whole list words per batch");
   constexpr int kWords = kBatch / 4;
+  const uint64_t pol = l2_evict_first();
   for (uint32_t e0 = 0; e0 < cnt; e0 += kBatch) {
     uint32_t slot[kBatch];
     // the next batch's list words, on their way to L2 while this one computes
@@ -139,7 +143,7 @@ __device__ __forceinline__ void for_each_listed(const NbrCtx &c, uint32_t k, uin
 #pragma unroll
     for (int w = 0; w < kWords; ++w) {
       const uint32_t g = (e0 >> 2) + (uint32_t)w;
-      const uint4 v = (w == 0 || 4u * g < cnt) ? load_list_word(&c.nbr4[(size_t)g * c.n + k])
+      const uint4 v = (w == 0 || 4u * g < cnt) ? load_list_word(&c.nbr4[(size_t)g * c.n + k], pol)
                                                 : make_uint4(k, k, k, k);
       slot[4 * w + 0] = v.x;
       slot[4 * w + 1] = v.y;
@@ -162,17 +166,18 @@ __device__ __forceinline__ void for_each_listed_ahead(const NbrCtx &c, uint32_t 
                                                       uint32_t cnt, Load &&load, F &&f) {
   static_assert(kBatch % 4 == 0, "whole list words per batch");
   constexpr int kWords = kBatch / 4;
+  const uint64_t pol = l2_evict_first();
   uint4 cur[kWords];
 #pragma unroll
   for (int w = 0; w < kWords; ++w)
-    cur[w] = (w == 0 || 4u * (uint32_t)w < cnt) ? load_list_word(&c.nbr4[(size_t)w * c.n + k])
+    cur[w] = (w == 0 || 4u * (uint32_t)w < cnt) ? load_list_word(&c.nbr4[(size_t)w * c.n + k], pol)
                                                 : make_uint4(k, k, k, k);
   for (uint32_t e0 = 0; e0 < cnt; e0 += kBatch) {
     uint4 nxt[kWords];
 #pragma unroll
     for (int w = 0; w < kWords; ++w) {
       const uint32_t g = (e0 >> 2) + (uint32_t)(kWords + w);
-      nxt[w] = 4u * g < cnt ? load_list_word(&c.nbr4[(size_t)g * c.n + k])
+      nxt[w] = 4u * g < cnt ? load_list_word(&c.nbr4[(size_t)g * c.n + k], pol)
                             : make_uint4(k, k, k, k);
     }
     uint32_t slot[kBatch];
