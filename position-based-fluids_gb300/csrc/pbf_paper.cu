@@ -39,7 +39,7 @@
 // from L2, and the values a thread reads only for itself skip L1 as well, so
 // both caches keep the neighbour data that dozens of threads re-read (7%
 // off the whole step on GB300).  The next batch's list words are prefetched
-// into L2 (lambda, XSPH) or loaded into registers one batch ahead (delta-p,
+// into L2 (XSPH) or loaded into registers one batch ahead (lambda, delta-p,
 // vorticity, whose register budgets allow it), so a batch's neighbour loads
 // do not wait on a list word from DRAM.
 //
@@ -269,8 +269,8 @@ __device__ __forceinline__ void visit_fallback(const NbrCtx &c, uint32_t k, F &&
 // path, for k itself as the padding of the last group): from the list when
 // k's set fits, otherwise re-derived.  kAhead selects the list
 // walk that holds the next batch's words in registers: measured faster for
-// delta-p and vorticity, slower for lambda and XSPH (whose register budgets
-// it overruns).
+// lambda, delta-p and vorticity, slower for XSPH (whose register budget it
+// overruns).
 template <int kBatch, bool kAhead = false, typename Load, typename F>
 __device__ __forceinline__ void visit_neighbours(const NbrCtx &c, uint32_t k, Load &&load,
                                                  F &&f) {
@@ -514,7 +514,7 @@ __global__ void __launch_bounds__(kBlock)
   if (k >= c.n) return;
   const float4 pk = P[k];
   LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
-  visit_neighbours<kBatch>(
+  visit_neighbours<kBatch, true>(
       nc, k, [&](uint32_t j) { return __ldg(&P[j]); },
       [&](float4 pj) {
         const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
