@@ -119,7 +119,7 @@ const char *pbf_last_error_message(void);
 
 /* Defaults: mode PAPER, 4 iterations, relax_eps 600, s_corr k 0.1 n 4
  * dq 0.2, XSPH c 0.01, vorticity eps 0.0005, gravity -9.81, wall margin
- * h/4 (resolved at create time when negative), max_neighbours 64. */
+ * h/4 (resolved at create time when negative), max_neighbours 128. */
 void pbf_params_default(pbf_params *p);
 
 /* ------------------------------------------------ scenario layer (L0) */

@@ -224,7 +224,7 @@ void pbf_params_default(pbf_params *p) {
   p->vort_eps = 0.0005f;
   p->gravity_y = -9.81f;
   p->wall_margin = -1.0f; /* resolved to h/4 */
-  p->max_neighbours = 64;
+  p->max_neighbours = 128;
 }
 
 }  // extern "C"

@@ -59,7 +59,7 @@ def base_params(box, cells, mode: int = MODE_PAPER) -> Params:
     p.vort_eps = 0.0005
     p.gravity_y = -9.81
     p.wall_margin = 0.25 * H
-    p.max_neighbours = 64
+    p.max_neighbours = 128
     return p
 
 

@@ -45,7 +45,7 @@ def test_params_defaults(pbf):
     assert p.scorr_k == pytest.approx(0.1) and p.scorr_n == 4 and p.scorr_dq == pytest.approx(0.2)
     assert p.xsph_c == pytest.approx(0.01) and p.vort_eps == pytest.approx(0.0005)
     assert p.gravity_y == pytest.approx(-9.81)
-    assert p.max_neighbours == 64
+    assert p.max_neighbours == 128
 
 
 PAR_TEXT = """part_input_file       two.in
