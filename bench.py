@@ -47,7 +47,9 @@ requests solved one at a time on the plain path.
 I/O text vs binary, the headless runner's snapshot cost, a 1280 x 720
 render), printed as one line with "metric": "aux".
 --save-state / --load-state write and resume the single scene's state (for
-profiling a late state of the simulation).
+profiling a late state of the simulation); --max-neighbours sets the
+neighbour-list capacity of the single and large scenes (particles with more
+neighbours re-derive their sets in every pass).
 
 --impl reference times the reference's own CPU implementation on the same
 workload and prints the same line with "impl": "reference".
@@ -306,6 +308,8 @@ def run_ours(args) -> int:
     dist = make_group(world, "nccl")
     pbf = ge.load_package()
     sc = pbf.scenes.config_4m() if args.workload == "large" else pbf.scenes.config_1m()
+    if args.max_neighbours:
+        sc.params.max_neighbours = args.max_neighbours
     n = sc.n
     sim = pbf.Simulation(sc.params, sc.particles)
     sim.init()
@@ -416,6 +420,7 @@ def run_ours(args) -> int:
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set larger than L2; no flush between steps",
                        "graph": True, "start_state": args.load_state or "initial block",
+                       "list_capacity": int(sc.params.max_neighbours),
                        "tuning": tuning},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * nbytes,
                     "d2h_bytes_per_step": 2 * nbytes, "steps": e2e_steps, "finite": finite},
@@ -804,6 +809,8 @@ def main() -> int:
                     help="single scene: write the state after the warm-up and timed steps (.npz)")
     ap.add_argument("--load-state", default=None,
                     help="single scene: start from a state written by --save-state")
+    ap.add_argument("--max-neighbours", type=int, default=None,
+                    help="single and large scenes: neighbour-list capacity (default: the scene's)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -138,7 +138,9 @@ enum GatherKind : int {
 // variant computes each particle in one thread with the same operations in
 // the same order.
 struct GatherTuning {
-  uint8_t block[kGatherKinds] = {1, 1, 1, 1, 1, 1};  // threads per CTA: 64 << code
+  // threads per CTA, 64 << code: 128, except 256 for lambda and vorticity
+  // (fastest over the 1M-particle dam break's 500 steps)
+  uint8_t block[kGatherKinds] = {1, 1, 2, 1, 2, 1};
   uint8_t batch[kGatherKinds] = {0, 0, 0, 0, 0, 0};  // neighbour loads in flight: 4 << code
   uint8_t fuse_first = 0;  // 1: one kernel builds the lists and computes the first lambda
 };

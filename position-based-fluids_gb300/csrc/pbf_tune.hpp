@@ -14,11 +14,18 @@ namespace pbf {
 // Times every launch shape (threads per CTA x neighbour loads in flight x
 // list build fused with the first lambda or not) over `trials` steps, each
 // shape from the same state, and keeps for every gather pass the shape with
-// the shortest launches.  X, V and ID of the first n slots are saved before
-// and restored after, so the caller's state is unchanged; since no shape
-// changes a result bit, later steps are the ones an untuned run would take.
+// the shortest launches.  The current shapes are timed first and a pass
+// moves to another shape only when that one is more than kTuneMargin
+// faster: on a near-tie the pick would follow timing noise, and the
+// defaults are the shapes measured fastest over a whole dam break, where
+// later states separate shapes that tie on the starting lattice.  X, V and
+// ID of the first n slots are saved before and restored after, so the
+// caller's state is unchanged; since no shape changes a result bit, later
+// steps are the ones an untuned run would take.
 // `step()` launches one step eagerly on `st` and returns a pbf_status.
 // per_launch_ms[k] receives the best time of kind k (0 if never launched).
+constexpr double kTuneMargin = 0.01;
+
 template <typename Step>
 int paper_autotune(DeviceState &d, uint32_t n, cudaStream_t st, uint32_t trials, Step &&step,
                    double per_launch_ms[kGatherKinds]) {
@@ -56,35 +63,52 @@ int paper_autotune(DeviceState &d, uint32_t n, cudaStream_t st, uint32_t trials,
   GatherTuning best = before;
   double best_ms[kGatherKinds];
   for (int k = 0; k < kGatherKinds; ++k) best_ms[k] = std::numeric_limits<double>::infinity();
+  // Runs `trials` steps (one, untimed, when !timed) with shapes t from the
+  // saved state; when timed, a pass takes t's shape if it is the first
+  // timing of that pass (incumbent) or beats the best by the margin.
+  auto trial = [&](const GatherTuning &t, bool timed, bool incumbent) {
+    if (!copy_state(false)) return false;
+    d.tune = t;
+    d.timer = timed ? timer : nullptr;
+    const uint32_t steps = timed ? trials : 1u;
+    for (uint32_t i = 0; i < steps && rc == PBF_OK; ++i) rc = step();
+    d.timer = nullptr;
+    if (rc != PBF_OK) return false;
+    if (!timed) return true;
+    double ms[kGatherKinds];
+    uint32_t cnt[kGatherKinds];
+    if (!cuda(timer->collect(ms, cnt), "tune timing")) return false;
+    for (int k = 0; k < kGatherKinds; ++k) {
+      if (!cnt[k]) continue;
+      const double tk = ms[k] / cnt[k];
+      const bool first = best_ms[k] == std::numeric_limits<double>::infinity();
+      if ((incumbent && first) || tk < best_ms[k] * (1.0 - kTuneMargin)) {
+        best_ms[k] = tk;
+        best.block[k] = t.block[k];
+        best.batch[k] = t.batch[k];
+      }
+    }
+    return true;
+  };
   if (cuda(cudaMalloc(&sx, (size_t)n * sizeof(float4)), "tune alloc") &&
       cuda(cudaMalloc(&sv, (size_t)n * sizeof(float4)), "tune alloc") &&
       cuda(cudaMalloc(&sid, (size_t)n * sizeof(uint32_t)), "tune alloc") &&
       cuda(timer->init(), "tune events") && copy_state(true)) {
     for (int pass = 0; pass < 2 && rc == PBF_OK; ++pass) {
-      // pass 0 loads every variant once (untimed); pass 1 times them
+      // pass 0 loads every variant once (untimed); pass 1 times the current
+      // shapes (split and fused) first, then every uniform shape
+      const bool timed = pass == 1;
+      if (timed) {
+        GatherTuning cur = before;
+        for (int fuse = 0; fuse < 2 && rc == PBF_OK; ++fuse) {
+          cur.fuse_first = (uint8_t)fuse;
+          if (!trial(cur, true, true)) break;
+        }
+      }
       for (int fuse = 0; fuse < 2 && rc == PBF_OK; ++fuse)
         for (int bl = 0; bl < kBlockCodes && rc == PBF_OK; ++bl)
-          for (int nb = 0; nb < kBatchCodes && rc == PBF_OK; ++nb) {
-            if (!copy_state(false)) break;
-            d.tune = uniform(bl, nb, fuse);
-            d.timer = pass == 1 ? timer : nullptr;
-            const uint32_t steps = pass == 1 ? trials : 1u;
-            for (uint32_t i = 0; i < steps && rc == PBF_OK; ++i) rc = step();
-            d.timer = nullptr;
-            if (rc != PBF_OK || pass == 0) continue;
-            double ms[kGatherKinds];
-            uint32_t cnt[kGatherKinds];
-            if (!cuda(timer->collect(ms, cnt), "tune timing")) break;
-            for (int k = 0; k < kGatherKinds; ++k) {
-              if (!cnt[k]) continue;
-              const double t = ms[k] / cnt[k];
-              if (t < best_ms[k]) {
-                best_ms[k] = t;
-                best.block[k] = (uint8_t)bl;
-                best.batch[k] = (uint8_t)nb;
-              }
-            }
-          }
+          for (int nb = 0; nb < kBatchCodes && rc == PBF_OK; ++nb)
+            if (!trial(uniform(bl, nb, fuse), timed, false)) break;
     }
     if (rc == PBF_OK) {
       best.fuse_first =
