@@ -22,6 +22,8 @@ Our arm prints one JSON line with:
   density_error  the density constraint's error in the final state
             (mean and max compression, interior mean |rho/rho0 - 1|), read
             back after the timed region;
+  neighbour_lists  the final step's largest neighbour count and how many
+            particles exceeded the list capacity (and re-derived their sets);
   cpu_baseline  the reference's own kernels (compiled from their sources)
             or, where they are absent, the oracle's restatement of them, on a
             bounded sample of the same workload on the host cores.
@@ -342,6 +344,7 @@ def run_ours(args) -> int:
     if args.save_state and rank == 0:
         sim.save_state(args.save_state)
     density_error = density_error_of(sim, sc.params.rest_density, args.warmup + args.steps)
+    nbr_max, nbr_over = sim.neighbour_stats()
 
     # ---- end to end through the C-ABI with host buffers ------------------
     nbytes = n * 16
@@ -432,6 +435,8 @@ def run_ours(args) -> int:
             "kernel_ms_per_step": {k: v[0] / kt_steps for k, v in kt.items()},
             "clocks": clock_summary,
             "density_error": density_error,
+            "neighbour_lists": {"capacity": int(sc.params.max_neighbours), "max_count": nbr_max,
+                                "overflow": nbr_over, "at_step": args.warmup + args.steps},
             "cpu_baseline": cpu,
             "ref_equations": ref_eq,
         }

@@ -242,6 +242,13 @@ int pbf_set_tuning(pbf_sim *sim, const pbf_tuning *tuning);
 /* Density of every particle from the last lambda pass of the last step
  * (input order). */
 int pbf_get_density(pbf_sim *sim, float *density);
+/* Neighbour lists of the last step (PAPER mode): the largest neighbour
+ * count and how many particles had more neighbours than the list capacity
+ * (max_neighbours rounded down to a multiple of 8).  Those particles
+ * re-derive their sets from the cells in every pass, several times as slow
+ * as a listed set; a nonzero *overflow says the capacity is too small for
+ * the scene.  PBF_ERR_STATE in REF_COMPAT mode or before the first step. */
+int pbf_neighbour_stats(pbf_sim *sim, uint32_t *max_count, uint32_t *overflow);
 /* The neighbour structure the last step built, in input particle order:
  * hash[i] = cell of particle i; perm[q] = input index of the particle at
  * sorted position q (ties by input index in REF_COMPAT mode, by previous

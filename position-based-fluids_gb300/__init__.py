@@ -192,6 +192,7 @@ def lib():
             "pbf_set_graph": ([vp, i32], i32),
             "pbf_launches_per_step": ([vp, C.POINTER(u32)], i32),
             "pbf_get_density": ([vp, vp], i32),
+            "pbf_neighbour_stats": ([vp, C.POINTER(u32), C.POINTER(u32)], i32),
             "pbf_get_cells": ([vp, vp, vp, vp], i32),
             "pbf_destroy": ([vp], i32),
             "pbf_autotune": ([vp, u32, C.POINTER(Tuning)], i32),
@@ -416,6 +417,13 @@ class Simulation:
         out = np.zeros(self.n, np.float32)
         _check(lib().pbf_get_density(self._h, _ptr(out)), "pbf_get_density")
         return out
+
+    def neighbour_stats(self) -> tuple[int, int]:
+        """(largest neighbour count, particles over the list capacity) of the
+        last step's neighbour lists."""
+        mx, over = C.c_uint32(), C.c_uint32()
+        _check(lib().pbf_neighbour_stats(self._h, C.byref(mx), C.byref(over)), "pbf_neighbour_stats")
+        return mx.value, over.value
 
     def cells(self):
         """(hash per particle, sorted permutation, inclusive ranges per cell)."""

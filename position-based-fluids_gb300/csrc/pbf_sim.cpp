@@ -595,6 +595,23 @@ int pbf_get_density(pbf_sim *s, float *density) {
   return PBF_OK;
 }
 
+int pbf_neighbour_stats(pbf_sim *s, uint32_t *max_count, uint32_t *overflow) {
+  if (!ready(s) || !max_count || !overflow) return ready(s) ? PBF_ERR_INVALID : PBF_ERR_STATE;
+  if (!s->paper || !s->stepped) return PBF_ERR_STATE;
+  std::vector<uint32_t> cnt(s->n);
+  PBF_TRY(cudaMemcpyAsync(cnt.data(), s->d.nbr_cnt, (size_t)s->n * sizeof(uint32_t),
+                          cudaMemcpyDeviceToHost, s->stream));
+  PBF_TRY(cudaStreamSynchronize(s->stream));
+  uint32_t mx = 0, over = 0;
+  for (uint32_t c : cnt) {
+    mx = c > mx ? c : mx;
+    over += c > s->pc.maxn ? 1u : 0u;
+  }
+  *max_count = mx;
+  *overflow = over;
+  return PBF_OK;
+}
+
 int pbf_get_cells(pbf_sim *s, uint32_t *hash, uint32_t *perm, int32_t *ranges) {
   if (!ready(s)) return PBF_ERR_STATE;
   if (!s->stepped) return PBF_ERR_STATE;

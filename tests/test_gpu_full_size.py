@@ -108,14 +108,18 @@ def test_single_scene_1m_density_over_500_steps(pbf):
     relaxation 600 are soft, so the impact (steps 60-160) compresses more.
     Measured: worst mean compression 0.264, worst max 3.32 (one particle in
     the splash), worst interior mean |rho/rho0 - 1| 0.266, settled mean
-    compression after step 400 0.015.  Stated bounds, ~30% above."""
+    compression after step 400 0.015.  Stated bounds, ~30% above.  The
+    same samples check the neighbour lists: no particle exceeds the default
+    list capacity (128), so none re-derives its set in the passes."""
     sc = pbf.scenes.config_1m()
     rho0 = sc.params.rest_density
     stats = []
+    nbr = []
     with pbf.Simulation(sc.params, sc.particles) as sim:
         sim.init()
         for k in range(50):
             sim.step(10)
+            nbr.append(sim.neighbour_stats())
             rho = sim.density() / rho0
             comp = np.maximum(rho - 1.0, 0.0)
             interior = rho >= 0.8
@@ -127,10 +131,13 @@ def test_single_scene_1m_density_over_500_steps(pbf):
     print(json.dumps({"density_error_500_steps_1m": {"mean_compression": worst[0],
                                                      "max_compression": worst[1],
                                                      "mean_abs_interior": worst[2],
-                                                     "settled_mean_compression": late}}))
+                                                     "settled_mean_compression": late},
+                      "neighbour_lists": {"max_count": max(m for m, _ in nbr),
+                                          "overflow": max(o for _, o in nbr)}}))
     assert inside_walls(sc.params, pos)
     assert worst[0] <= 0.35 and worst[1] <= 4.5 and worst[2] <= 0.35
     assert late <= 0.02
+    assert max(o for _, o in nbr) == 0
 
 
 def test_double_dam_break_4m_step_vs_fp64_oracle(pbf, oracle_mod):
