@@ -38,10 +38,9 @@
 // once) are loaded without allocating in L1 and first in line for eviction
 // from L2, and the values a thread reads only for itself skip L1 as well, so
 // both caches keep the neighbour data that dozens of threads re-read (7%
-// off the whole step on GB300).  The next batch's list words are prefetched
-// into L2 (XSPH) or loaded into registers one batch ahead (lambda, delta-p,
-// vorticity, whose register budgets allow it), so a batch's neighbour loads
-// do not wait on a list word from DRAM.
+// off the whole step on GB300).  The next batch's list words are loaded into
+// registers one batch ahead, so a batch's neighbour loads do not wait on a
+// list word from DRAM.
 //
 // Measured on GB300 (1M-particle dam break after 500 steps, per step):
 // absolute 32-bit entries run 9% faster than 16-bit entries relative to a
@@ -122,48 +121,14 @@ __device__ __forceinline__ float load_own(const float *p) {
 // For the `cnt` listed neighbours of particle k, kBatch (4 or 8) at a time:
 // the batch's list words, then load(slot) for every entry of the batch, then
 // f(data) for each in list order -- the loads of a batch are in flight
-// together.  The list build pads the last word with k's own slot and words
-// past the count read as k: those entries are the particle itself, which
-// every pass drops through the pair test (r^2 = 0), so no entry needs a
-// bound or a count test.
+// together, and the next batch's list words are loaded into registers while
+// the current batch's neighbour data loads and computes.  The list build
+// pads the last word with k's own slot and words past the count read as k:
+// those entries are the particle itself, which every pass drops through the
+// pair test (r^2 = 0), so no entry needs a bound or a count test.
 template <int kBatch, typename Load, typename F>
 __device__ __forceinline__ void for_each_listed(const NbrCtx &c, uint32_t k, uint32_t cnt,
                                                 Load &&load, F &&f) {
-  static_assert(kBatch % 4 == 0, "whole list words per batch");
-  constexpr int kWords = kBatch / 4;
-  const uint64_t pol = l2_evict_first();
-  for (uint32_t e0 = 0; e0 < cnt; e0 += kBatch) {
-    uint32_t slot[kBatch];
-    // the next batch's list words, on their way to L2 while this one computes
-#pragma unroll
-    for (int w = 0; w < kWords; ++w) {
-      const uint32_t g = (e0 >> 2) + (uint32_t)(kWords + w);
-      if (4u * g < cnt) asm volatile("prefetch.global.L2 [%0];" ::"l"(&c.nbr4[(size_t)g * c.n + k]));
-    }
-#pragma unroll
-    for (int w = 0; w < kWords; ++w) {
-      const uint32_t g = (e0 >> 2) + (uint32_t)w;
-      const uint4 v = (w == 0 || 4u * g < cnt) ? load_list_word(&c.nbr4[(size_t)g * c.n + k], pol)
-                                                : make_uint4(k, k, k, k);
-      slot[4 * w + 0] = v.x;
-      slot[4 * w + 1] = v.y;
-      slot[4 * w + 2] = v.z;
-      slot[4 * w + 3] = v.w;
-    }
-    decltype(load(0u)) data[kBatch];
-#pragma unroll
-    for (int e = 0; e < kBatch; ++e) data[e] = load(slot[e]);
-#pragma unroll
-    for (int e = 0; e < kBatch; ++e) f(data[e]);
-  }
-}
-
-// for_each_listed with the same entries, order and calls of f, but the next
-// batch's list words are loaded into registers while the current batch's
-// neighbour data loads and computes (four more live registers per thread).
-template <int kBatch, typename Load, typename F>
-__device__ __forceinline__ void for_each_listed_ahead(const NbrCtx &c, uint32_t k,
-                                                      uint32_t cnt, Load &&load, F &&f) {
   static_assert(kBatch % 4 == 0, "whole list words per batch");
   constexpr int kWords = kBatch / 4;
   const uint64_t pol = l2_evict_first();
@@ -267,17 +232,13 @@ __device__ __forceinline__ void visit_fallback(const NbrCtx &c, uint32_t k, F &&
 
 // Calls f(load(slot)) for every neighbour of particle k (and, in the listed
 // path, for k itself as the padding of the last group): from the list when
-// k's set fits, otherwise re-derived.  kAhead selects the list
-// walk that holds the next batch's words in registers: measured faster for
-// lambda, delta-p and vorticity, slower for XSPH (whose register budget it
-// overruns).
-template <int kBatch, bool kAhead = false, typename Load, typename F>
+// k's set fits, otherwise re-derived.
+template <int kBatch, typename Load, typename F>
 __device__ __forceinline__ void visit_neighbours(const NbrCtx &c, uint32_t k, Load &&load,
                                                  F &&f) {
   const uint32_t cnt = load_own(&c.cnt[k]);
   if (cnt <= c.maxn) {
-    if constexpr (kAhead) for_each_listed_ahead<kBatch>(c, k, cnt, load, f);
-    else for_each_listed<kBatch>(c, k, cnt, load, f);
+    for_each_listed<kBatch>(c, k, cnt, load, f);
   } else {
     visit_fallback(c, k, [&](uint32_t j) { f(load(j)); });
   }
@@ -514,7 +475,7 @@ __global__ void __launch_bounds__(kBlock)
   if (k >= c.n) return;
   const float4 pk = P[k];
   LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
-  visit_neighbours<kBatch, true>(
+  visit_neighbours<kBatch>(
       nc, k, [&](uint32_t j) { return __ldg(&P[j]); },
       [&](float4 pj) {
         const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
@@ -536,7 +497,7 @@ __global__ void __launch_bounds__(kBlock)
   float sx = 0.f, sy = 0.f, sz = 0.f;
   // one neighbour walk per s_corr exponent form, chosen once per thread
   const auto walk = [&](auto twelve) {
-    visit_neighbours<kBatch, true>(
+    visit_neighbours<kBatch>(
         nc, k, [&](uint32_t j) { return __ldg(&Q[j]); },
         [&](float4 qj) {
           const float rx = qk.x - qj.x, ry = qk.y - qj.y, rz = qk.z - qj.z;
@@ -587,7 +548,7 @@ __global__ void __launch_bounds__(kBlock)
   struct PU {
     float4 p, u;
   };
-  visit_neighbours<kBatch, true>(
+  visit_neighbours<kBatch>(
       nc, k, [&](uint32_t j) { return PU{__ldg(&P[j]), __ldg(&U[j])}; },
       [&](const PU &d) {
     const float4 pj = d.p;
@@ -608,12 +569,11 @@ __global__ void __launch_bounds__(kBlock)
   PW[k] = make_float4(pk.x, pk.y, pk.z, wn);
 }
 
-// At least 1152 resident threads per SM with four loads in flight (56
-// registers; 64 at 256 threads), 1024 with eight (64 registers): no spills
-// in any shape.  Left to itself the compiler takes 63 (96 with eight loads
-// in flight) and halves the resident warps.
+// At least 1024 resident threads per SM (64 registers): no spills in any
+// shape.  Left to itself the compiler takes more (96 with eight loads in
+// flight) and halves the resident warps.
 template <int kBlock, int kBatch>
-__global__ void __launch_bounds__(kBlock, (kBatch == 8 ? 1024 : 1152) / kBlock)
+__global__ void __launch_bounds__(kBlock, 1024 / kBlock)
     k_xsph_commit(const float4 *__restrict__ PW, const float4 *__restrict__ U,
                   const float4 *__restrict__ Wv, NbrCtx nc, PaperConsts c,
                   const uint32_t *__restrict__ ID2, float4 *__restrict__ X,
