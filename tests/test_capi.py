@@ -184,6 +184,9 @@ def test_create_validation(pbf):
     with pytest.raises(pbf.PbfError) as e:
         s.step(1, sync=False)
     assert e.value.status == pbf.ERR_STATE
+    with pytest.raises(pbf.PbfError) as e:
+        s.neighbour_stats()
+    assert e.value.status == pbf.ERR_STATE
     s.close()
 
 
