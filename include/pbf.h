@@ -315,6 +315,10 @@ int pbf_batch_info(const pbf_batch *b, uint32_t *scenes, uint32_t *particles,
                    uint32_t *cells);
 int pbf_batch_get_stream(const pbf_batch *b, void **stream);
 int pbf_batch_launches_per_step(const pbf_batch *b, uint32_t *launches);
+/* pbf_neighbour_stats over every scene of the batch (the last step's
+ * lists); PBF_ERR_STATE until a step has run since the last add or
+ * remove. */
+int pbf_batch_neighbour_stats(pbf_batch *b, uint32_t *max_count, uint32_t *overflow);
 /* pbf_autotune for a batch, over the scenes it holds. */
 int pbf_batch_autotune(pbf_batch *b, uint32_t trial_steps, pbf_tuning *out);
 int pbf_batch_get_tuning(const pbf_batch *b, pbf_tuning *out);

@@ -223,6 +223,7 @@ def lib():
             "pbf_batch_info": ([vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)], i32),
             "pbf_batch_get_stream": ([vp, C.POINTER(vp)], i32),
             "pbf_batch_launches_per_step": ([vp, C.POINTER(u32)], i32),
+            "pbf_batch_neighbour_stats": ([vp, C.POINTER(u32), C.POINTER(u32)], i32),
             "pbf_batch_destroy": ([vp], i32),
             "pbf_server_create": ([pp, C.c_uint64, u32, f32, u32, C.POINTER(vp)], i32),
             "pbf_server_submit": ([vp, pp, vp, u32, u32, C.POINTER(C.c_uint64)], i32),
@@ -579,6 +580,14 @@ class Batch:
         n = C.c_uint32()
         _check(lib().pbf_batch_launches_per_step(self._h, C.byref(n)), "pbf_batch_launches_per_step")
         return n.value
+
+    def neighbour_stats(self) -> tuple[int, int]:
+        """(largest neighbour count, particles over the list capacity) of the
+        last step's neighbour lists, over every scene."""
+        mx, over = C.c_uint32(), C.c_uint32()
+        _check(lib().pbf_batch_neighbour_stats(self._h, C.byref(mx), C.byref(over)),
+               "pbf_batch_neighbour_stats")
+        return mx.value, over.value
 
     def autotune(self, trial_steps: int = 3) -> Tuning:
         t = Tuning()

@@ -443,6 +443,26 @@ int pbf_batch_launches_per_step(const pbf_batch *b, uint32_t *launches) {
   return PBF_OK;
 }
 
+int pbf_batch_neighbour_stats(pbf_batch *b, uint32_t *max_count, uint32_t *overflow) {
+  if (!b || !max_count || !overflow) return PBF_ERR_INVALID;
+  // the lists belong to the current layout only after a step ran on it
+  if (!b->graph || b->graph_stale || b->dirty) return PBF_ERR_STATE;
+  std::vector<uint32_t> cnt(b->n_total);
+  if (b->n_total) {
+    PBF_TRY(cudaMemcpyAsync(cnt.data(), b->d.nbr_cnt, (size_t)b->n_total * sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, b->stream));
+    PBF_TRY(cudaStreamSynchronize(b->stream));
+  }
+  uint32_t mx = 0, over = 0;
+  for (uint32_t c : cnt) {
+    mx = c > mx ? c : mx;
+    over += c > b->pc.maxn ? 1u : 0u;
+  }
+  *max_count = mx;
+  *overflow = over;
+  return PBF_OK;
+}
+
 int pbf_batch_autotune(pbf_batch *b, uint32_t trial_steps, pbf_tuning *out) {
   if (!b || trial_steps < 1 || trial_steps > 32) return PBF_ERR_INVALID;
   if (b->dirty) PBF_TRY_STATUS(apply_layout(b));

@@ -74,6 +74,36 @@ def test_batch_matches_plain_simulation_bitwise(pbf):
         assert_same(g, run_plain(pbf, s, 25), f"scene {s.name}")
 
 
+def test_batch_neighbour_stats_match_the_plain_simulations(pbf):
+    """The batch's list statistics are those of its scenes stepped alone
+    (largest count the largest of theirs, overflows their sum), also with a
+    capacity small enough that some particles overflow; none before a step
+    on the current layout."""
+    scenes = plain_scenes(pbf)
+    for cap in (128, 16):
+        solver = scenes[0].params.copy()
+        solver.max_neighbours = cap
+        alone = []
+        for s in scenes:
+            p = s.params.copy()
+            p.max_neighbours = cap
+            with pbf.Simulation(p, s.particles) as sim:
+                sim.init()
+                sim.step(5)
+                alone.append(sim.neighbour_stats())
+        with pbf.Batch(solver, *capacity(scenes)) as b:
+            for s in scenes:
+                b.add_scene(s.params, s.particles)
+            with pytest.raises(pbf.PbfError) as e:
+                b.neighbour_stats()
+            assert e.value.status == pbf.ERR_STATE
+            b.step(5)
+            mx, over = b.neighbour_stats()
+        assert mx == max(m for m, _ in alone)
+        assert over == sum(o for _, o in alone)
+        assert (over > 0) == (cap == 16)
+
+
 def test_mixed_sizes_alone_vs_mix_bitwise(pbf):
     scenes = pbf.scenes.mixed_batch(count=8, n_min=1000, n_max=30000, seed=7)
     solver = scenes[0].params
