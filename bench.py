@@ -24,9 +24,20 @@ Our arm prints one JSON line with:
             back after the timed region;
   neighbour_lists  the final step's largest neighbour count and how many
             particles exceeded the list capacity (and re-derived their sets);
+  fp64_step_error  one more step from the final state against the FP64
+            oracle of the same equations from the same state (largest
+            position difference in h; the bound is 1e-5 h), untimed;
+  equations "paper": the line's value runs Macklin & Mueller's equations;
+  ref_equations  the same scene in REF_COMPAT mode (the reference kernels'
+            own equations, bit-exact with them): device-resident and end to
+            end through the C-ABI with host buffers, steps 1..20 from the
+            initial state -- the like-for-like figure beside the reference
+            arm, which can only run the reference's equations;
   cpu_baseline  the reference's own kernels (compiled from their sources)
             or, where they are absent, the oracle's restatement of them, on a
-            bounded sample of the same workload on the host cores.
+            bounded sample of the same workload on the host cores (the scene
+            built by the oracle's own generator: the CPU legs load nothing of
+            the product library).
 The working set (state, neighbour lists, sort buffers) is several hundred MB,
 larger than L2, so no flush runs between steps.
 
@@ -85,10 +96,13 @@ UNIT = "particle-iterations/s"
 # cell ranges 8, reorder 104, lambda 24, delta-p 36, vorticity 48,
 # XSPH+commit 84; 608 per particle-step in total.  The neighbour-list build
 # (read p* 16, write the count 4) is an implementation choice outside that
-# total.
+# total; fused with the first lambda it counts both (20 + 24).  Every kernel
+# the step launches has an entry, so the roofline object names the kernel
+# that takes the most time.
 ALG_BYTES = {
     "predict_hash": 72, "sort_onesweep": 52, "cell_offsets": 8, "reorder": 104,
-    "nbr_build": 20, "lambda": 24, "delta": 36, "vorticity": 48, "xsph_commit": 84,
+    "nbr_build": 20, "nbr_lambda": 44, "lambda": 24, "delta": 36, "vorticity": 48,
+    "xsph_commit": 84,
 }
 STEP_BYTES = 608
 
@@ -206,21 +220,68 @@ def reduce_max(dist, value: float, device=None) -> float:
     return float(t.item())
 
 
-def cpu_reference_run(n_steps_max: int = 50, budget_s: float = 15.0, threads: int = 0,
-                      scene=None):
-    """Times the reference's own kernels (or the oracle restatement where
-    they are not built) on the workload's scene (the 1M scene unless given),
-    one step at a time until `budget_s` of CPU time is spent.  Returns
-    (value, info)."""
-    import oracle
-    import __graft_entry__ as ge
+class EventTimer:
+    """Device time on one CUDA stream (events recorded on it)."""
 
-    pbf = ge.load_package()
-    sc = scene if scene is not None else pbf.scenes.config_1m()
-    p = sc.params
-    cfg = oracle.Config(p.x_min, p.x_max, p.y_min, p.y_max, p.z_min, p.z_max, p.x_n, p.y_n, p.z_n,
-                        p.time_step_length, p.rest_density)
-    pos, vel = pbf.state_from_particles(sc.particles)
+    def __init__(self, stream):
+        import torch
+
+        self.stream = stream
+        self.e0 = torch.cuda.Event(enable_timing=True)
+        self.e1 = torch.cuda.Event(enable_timing=True)
+
+    def start(self):
+        self.e0.record(self.stream)
+
+    def stop(self) -> float:
+        self.e1.record(self.stream)
+        self.e1.synchronize()
+        return self.e0.elapsed_time(self.e1) / 1e3
+
+
+class WallTimer:
+    """Host wall time (for replicas whose step is not a CUDA stream)."""
+
+    def start(self):
+        self.t0 = time.perf_counter()
+
+    def stop(self) -> float:
+        return time.perf_counter() - self.t0
+
+
+def timed_replica_steps(dist, sim, steps: int, timer, particles: int, device=None,
+                        before=None) -> tuple[float, float]:
+    """Times `steps` steps of this rank's replica: a barrier over the ranks,
+    everything before it finished (`before`, e.g. torch.cuda.synchronize),
+    the steps enqueued between the timer's marks, then the slowest rank's
+    time.  Returns (seconds, value) with value = the particle-iterations of
+    every rank's replica over that time (replicas are independent: weak
+    scaling)."""
+    world = dist.get_world_size() if dist is not None else 1
+    if dist is not None:
+        dist.barrier()
+    if before is not None:
+        before()
+    sim.sync()
+    timer.start()
+    sim.step(steps, sync=False)
+    t = timer.stop()
+    sim.sync()
+    t = reduce_max(dist, t, device=device)
+    return t, world * particles * ITERATIONS * steps / t
+
+
+def cpu_reference_run(n_steps_max: int = 50, budget_s: float = 15.0, threads: int = 0,
+                      workload: str = "single"):
+    """Times the reference's own kernels (or the oracle restatement where
+    they are not built) on the workload's scene, one step at a time until
+    `budget_s` of CPU time is spent.  The scene comes from the oracle's own
+    generator (bit-identical to the library's, checked by the CPU tests), so
+    this leg loads nothing of the product library.  Returns (value, info)."""
+    import oracle
+
+    cfg, pos, vel = oracle.scene_4m() if workload == "large" else oracle.scene_1m()
+    n = pos.shape[0]
     threads = threads or (os.cpu_count() or 1)
     kind = "reference" if oracle.reference_available() else "port"
     steps = 0
@@ -234,9 +295,10 @@ def cpu_reference_run(n_steps_max: int = 50, budget_s: float = 15.0, threads: in
         if time.perf_counter() - t0 >= budget_s:
             break
     dt = time.perf_counter() - t0
-    value = sc.n * ITERATIONS * steps / dt
-    info = {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-            "sample": f"{steps} step(s) of the {sc.n}-particle scene from its initial state, "
+    value = n * ITERATIONS * steps / dt
+    info = {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "equations": "reference",
+            "steps": steps,
+            "sample": f"{steps} step(s) of the {n}-particle scene from its initial state, "
                       f"reference equations, {'reference kernels compiled from their .cl sources' if kind == 'reference' else 'oracle restatement of the reference kernels'}, "
                       f"{dt:.1f} s"}
     return value, info
@@ -247,13 +309,19 @@ def run_reference(args) -> int:
     world, rank, _ = dist_info()
     if rank != 0:
         return 0
-    value, info = cpu_reference_run(n_steps_max=max(1, args.steps), budget_s=args.cpu_budget)
+    value, info = cpu_reference_run(n_steps_max=max(1, args.steps), budget_s=args.cpu_budget,
+                                    workload=args.workload)
+    large = args.workload == "large"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "single_scene_1m", "particles": 1048576, "cells": 262144,
-                   "solver_iterations": ITERATIONS, "equations": "reference kernels"},
+        "equations": "reference",
+        "config": {"workload": "double_dam_break_4m" if large else "single_scene_1m",
+                   "particles": 4194304 if large else 1048576, "cells": 1048576 if large else 262144,
+                   "solver_iterations": ITERATIONS,
+                   "equations": "reference kernels (relaxation 1e4, no s_corr, XSPH, no vorticity)",
+                   "note": "the like-for-like GPU figure is the headline line's ref_equations"},
         "cpu_baseline": info,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -264,16 +332,25 @@ def run_reference(args) -> int:
 def ref_equations_run(pbf, sc, args) -> dict:
     """The same scene through the GPU path in REF_COMPAT mode (the
     reference's own equations, bit-exact with its kernels): the like-for-like
-    figure beside the reference arm, which runs those equations on the CPU."""
+    figure beside the reference arm, which runs those equations on the CPU.
+    Both legs time steps 1..20 from the scene's initial state, the sample the
+    CPU arm times: device-resident (CUDA graph steps, CUDA events), and end to
+    end through the C-ABI with page-locked host buffers (every step uploads
+    the state, steps and reads the state back inside the timed region)."""
+    import ctypes as C
+
     import torch
 
     p = sc.params.copy()
     p.mode = pbf.MODE_REF_COMPAT
-    warm, steps = 2, 20  # the first 22 steps, the sample the CPU reference arm times
+    steps = 20
+    pos0, vel0 = pbf.state_from_particles(sc.particles)
+    n = sc.n
     with pbf.Simulation(p, sc.particles) as sim:
         sim.init()
         sim.initCells()
-        sim.step(warm)
+        sim.step(2)  # module load, graph instantiation
+        sim.set_state(pos0, vel0)
         ext = torch.cuda.ExternalStream(sim.stream())
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -283,21 +360,66 @@ def ref_equations_run(pbf, sc, args) -> dict:
         e1.synchronize()
         sim.sync()
         t = e0.elapsed_time(e1) / 1e3
-        finite = bool(np.isfinite(sim.dumpData()[0]).all())
+        dev_pos, _ = sim.dumpData()
+        finite = bool(np.isfinite(dev_pos).all())
         launches = sim.launches_per_step()
-    first_bad = None
-    if not finite:  # which step first leaves the finite range (untimed)
-        with pbf.Simulation(p, sc.particles) as sim:
-            sim.init()
-            for k in range(1, warm + steps + 1):
-                sim.step(1)
-                if not np.isfinite(sim.dumpData()[0]).all():
-                    first_bad = k
-                    break
-    return {"value": sc.n * ITERATIONS * steps / t, "unit": UNIT, "ms_per_step": t / steps * 1e3,
-            "steps": steps, "warmup": warm, "gpu_launches": launches * steps, "finite": finite,
-            "first_nonfinite_step": first_bad,
-            "equations": "reference kernels' equations (REF_COMPAT), device-resident, CUDA graph"}
+        # end to end with host buffers
+        hp = pbf.lib()
+        nbytes = n * 16
+        pin_pos, pin_vel = C.c_void_p(), C.c_void_p()
+        hp.pbf_host_alloc(nbytes, C.byref(pin_pos))
+        hp.pbf_host_alloc(nbytes, C.byref(pin_vel))
+        host_pos = np.frombuffer((C.c_float * (4 * n)).from_address(pin_pos.value), np.float32).reshape(n, 4)
+        host_vel = np.frombuffer((C.c_float * (4 * n)).from_address(pin_vel.value), np.float32).reshape(n, 4)
+        host_pos[:] = pos0
+        host_vel[:] = vel0
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(ext)
+        for _ in range(steps):
+            sim.set_state_async(pin_pos.value, pin_vel.value)
+            sim.step(1, sync=False)
+            sim.dump_data_async(pin_pos.value, pin_vel.value)
+        f1.record(ext)
+        f1.synchronize()
+        sim.sync()
+        t_e2e = f0.elapsed_time(f1) / 1e3
+        same = bool(np.array_equal(host_pos.view(np.uint32), dev_pos.view(np.uint32)))
+        del host_pos, host_vel
+        hp.pbf_host_free(pin_pos)
+        hp.pbf_host_free(pin_vel)
+    return {"value": n * ITERATIONS * steps / t, "unit": UNIT, "ms_per_step": t / steps * 1e3,
+            "steps": steps, "start_state": "initial block", "gpu_launches": launches * steps,
+            "finite": finite, "equations": "reference",
+            "e2e": {"value": n * ITERATIONS * steps / t_e2e, "unit": UNIT,
+                    "ms_per_step": t_e2e / steps * 1e3, "h2d_bytes_per_step": 2 * nbytes,
+                    "d2h_bytes_per_step": 2 * nbytes, "same_result_as_device_resident": same},
+            "method": "REF_COMPAT (the reference kernels' equations, bit-exact with them), CUDA-graph "
+                      "steps 1..20 from the initial state; e2e through the C-ABI with page-locked "
+                      "host buffers, the state up and down every step"}
+
+
+def fp64_step_error(pbf, sim, params) -> dict:
+    """One more step of the simulation from its current state against the
+    FP64 oracle of the same equations from the same state (outside every
+    timed region): largest position and velocity difference, in h and m/s."""
+    import oracle
+    import __graft_entry__ as ge
+
+    pos, vel = sim.dumpData()
+    sim.set_state(pos, vel)
+    sim.step(1)
+    gpos, gvel = sim.dumpData()
+    t0 = time.perf_counter()
+    opos, ovel, *_ = oracle.paper_steps_f64(ge.paper_params_for_oracle(params), pos, vel, 1)
+    dx = np.abs(gpos[:, :3].astype(np.float64) - opos[:, :3]).max()
+    dv = np.abs(gvel[:, :3].astype(np.float64) - ovel[:, :3]).max()
+    return {"position_max_h": float(dx / params.h), "velocity_max": float(dv),
+            "bound_position_h": 1e-5, "within_bound": bool(dx <= 1e-5 * params.h),
+            "oracle_s": time.perf_counter() - t0,
+            "method": "one step from the state after the timed steps, GPU (binary32) against "
+                      "the FP64 oracle restatement of the same equations from the same state"}
 
 
 def run_ours(args) -> int:
@@ -319,6 +441,11 @@ def run_ours(args) -> int:
     if args.load_state:
         sim.load_state(args.load_state)
     tuning = None if args.no_tune else sim.autotune(3).as_dict()
+    if args.first_pass != "auto":
+        t = sim.tuning()
+        t.fuse_first = 1 if args.first_pass == "fused" else 0
+        sim.set_tuning(t)
+        tuning = sim.tuning().as_dict()
     ext = torch.cuda.ExternalStream(sim.stream())
     launches = sim.launches_per_step()
 
@@ -326,25 +453,15 @@ def run_ours(args) -> int:
     sim.step(args.warmup)
 
     # ---- device-resident throughput ------------------------------------
-    if dist is not None:
-        dist.barrier()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
-        e0.record(ext)
-        sim.step(args.steps, sync=False)
-        e1.record(ext)
-        e1.synchronize()
-    sim.sync()
-    t_dev = e0.elapsed_time(e1) / 1e3
-    t_dev = reduce_max(dist, t_dev, device="cuda")
-    value = world * n * ITERATIONS * args.steps / t_dev
+        t_dev, value = timed_replica_steps(dist, sim, args.steps, EventTimer(ext), n, device="cuda",
+                                           before=torch.cuda.synchronize)
     clock_summary = clocks.summary()
     if args.save_state and rank == 0:
         sim.save_state(args.save_state)
     density_error = density_error_of(sim, sc.params.rest_density, args.warmup + args.steps)
     nbr_max, nbr_over = sim.neighbour_stats()
+    fp64_err = fp64_step_error(pbf, sim, sc.params) if rank == 0 and not args.no_fp64 else None
 
     # ---- end to end through the C-ABI with host buffers ------------------
     nbytes = n * 16
@@ -407,7 +524,7 @@ def run_ours(args) -> int:
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        _, cpu = cpu_reference_run(budget_s=args.cpu_budget, scene=sc)
+        _, cpu = cpu_reference_run(budget_s=args.cpu_budget, workload=args.workload)
 
     sim.close()
     ref_eq = ref_equations_run(pbf, sc, args) if world == 1 else None
@@ -416,6 +533,7 @@ def run_ours(args) -> int:
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "equations": "paper",
             "config": {"workload": sc.name, "particles": n, "cells": sc.params.ncells,
                        "box": sc.meta["box"], "blocks": sc.meta.get("blocks", [sc.meta.get("block")]),
                        "solver_iterations": ITERATIONS,
@@ -435,6 +553,7 @@ def run_ours(args) -> int:
             "kernel_ms_per_step": {k: v[0] / kt_steps for k, v in kt.items()},
             "clocks": clock_summary,
             "density_error": density_error,
+            "fp64_step_error": fp64_err,
             "neighbour_lists": {"capacity": int(sc.params.max_neighbours), "max_count": nbr_max,
                                 "overflow": nbr_over, "at_step": args.warmup + args.steps},
             "cpu_baseline": cpu,
@@ -803,10 +922,15 @@ def main() -> int:
     ap.add_argument("--max-chunk", type=int, default=16, help="most batched steps per loop turn")
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU baseline work")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="skip the one-step comparison with the FP64 oracle after the timed steps")
     ap.add_argument("--plain-sample", type=int, default=30,
                     help="timed steps per scene of the one-by-one plain comparison")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-by-one plain comparison")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--first-pass", choices=["auto", "fused", "split"], default="auto",
+                    help="single and large scenes: list build fused with the first lambda pass, "
+                         "apart from it, or the tuner's (or default) choice")
     ap.add_argument("--forms", choices=["all", "none"], default="all",
                     help="single workload: also run the batched and served workloads and "
                          "summarise them in the line (one GPU only)")

@@ -417,11 +417,14 @@ int pbf_op_sort_status(const void *d_scratch, uint32_t n, uint32_t key_bits,
  * No counterpart in the reference.  Scratch is a file-scope device array
  * sized for at most 1048576 keys (about 9.4 MB on every GPU that loads the
  * library, held until exit); larger n returns PBF_ERR_INVALID.  The first
- * call on a device looks the array's address up (cudaGetSymbolAddress), so
- * make that first call before any stream capture.  All calls share the
- * array: calls whose work overlaps on the GPU race.  If d_status is not
- * NULL, look-back failures are OR-ed into *d_status (zeroed by the caller);
- * otherwise they are not reported. */
+ * call in a device's context looks the array's address up
+ * (cudaGetSymbolAddress), so make that first call before any stream
+ * capture; a later context on the same device (after cudaDeviceReset) is
+ * recognised by its id and looked up again on its first call.  All calls
+ * share the array: calls whose work overlaps on the GPU race.  If d_status
+ * is not NULL, look-back failures are OR-ed into *d_status (zeroed by the
+ * caller); otherwise they are not reported, so pass it wherever the result
+ * matters. */
 int pbf_op_sort_pairs_noalloc(const uint32_t *d_keys_in,
                               const uint32_t *d_vals_in, uint32_t n,
                               uint32_t key_bits, uint32_t *d_keys_out,

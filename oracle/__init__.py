@@ -179,6 +179,77 @@ def paper_steps_f64(prm: PaperParams, pos4, vel4, steps: int, wave: float = 0.0,
     return pos, vel, dens, lam, cnt
 
 
+# ----------------------------------------------------------- synthetic scenes
+# The benchmark scenes built on the oracle side, so that a CPU run of the
+# reference's kernels needs nothing from the product library.  The lattice
+# and jitter follow the product's seeded block generator (lattice order of
+# the reference's tools/gen_grid.py:1-49, x outermost and z innermost; three
+# splitmix64 draws per particle, x then y then z); tests check the two
+# bit for bit.
+_SPLITMIX_GAMMA = np.uint64(0x9E3779B97F4A7C15)
+
+
+def splitmix64(seed: int, count: int) -> np.ndarray:
+    """The first `count` outputs of Vigna's splitmix64 generator from state
+    `seed` (state += gamma, then the two xor-shift-multiply rounds)."""
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed & (2**64 - 1)) + _SPLITMIX_GAMMA * np.arange(1, count + 1, dtype=np.uint64)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def generate_block(origin, dims, spacing: float, jitter: float, mass: float, seed: int):
+    """(pos4, vel4) in the dumpData layout of a jittered lattice at rest:
+    x = origin + index * spacing + (2u - 1) * jitter per coordinate, u the
+    top 53 bits of a splitmix64 draw, evaluated in double and rounded once
+    to binary32 (origin, spacing and jitter are binary32 values)."""
+    nx, ny, nz = (int(d) for d in dims)
+    n = nx * ny * nz
+    idx = np.stack(np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij"),
+                   axis=-1).reshape(n, 3).astype(np.float64)
+    u = (splitmix64(seed, 3 * n) >> np.uint64(11)).astype(np.float64).reshape(n, 3) * (1.0 / 9007199254740992.0)
+    off = (2.0 * u - 1.0) * float(np.float32(jitter))
+    o = np.asarray(origin, np.float32).astype(np.float64)
+    pos = np.zeros((n, 4), np.float32)
+    pos[:, :3] = (o + idx * float(np.float32(spacing)) + off).astype(np.float32)
+    vel = np.zeros((n, 4), np.float32)
+    vel[:, 3] = np.float32(mass)
+    return pos, vel
+
+
+def dam_break_scene(dims, box, seed: int = 0x5EED):
+    """A benchmark dam break in the reference's units: a block at spacing
+    0.05 (h = 0.1) in the box's minimum corner, h/4 from each wall, jitter
+    0.01 spacing, mass 1000 * 0.05^3, cells of size h, dt = 1/120 and
+    number density 1/0.05^3.  Returns (Config, pos4, vel4)."""
+    h, spacing = 0.1, 0.05
+    cells = [int(round(b / h)) for b in box]
+    cfg = Config(0.0, box[0], 0.0, box[1], 0.0, box[2], cells[0], cells[1], cells[2],
+                 1.0 / 120.0, 1.0 / spacing ** 3)
+    m = 0.25 * h
+    pos, vel = generate_block((m, m, m), dims, spacing, 0.01 * spacing, 1000.0 * spacing ** 3, seed)
+    return cfg, pos, vel
+
+
+def scene_1m(seed: int = 0x5EED):
+    """The 1,048,576-particle headline scene (128 x 128 x 64 block, 6.4 m
+    cube, 64^3 cells)."""
+    return dam_break_scene((128, 128, 64), (6.4, 6.4, 6.4), seed)
+
+
+def scene_4m(seed: int = 0x5EED):
+    """The 4,194,304-particle double dam break: two 128^3 blocks on the floor
+    at opposite x ends of a 12.8 x 12.8 x 6.4 box (128 x 128 x 64 cells), the
+    second block seeded with seed + 1."""
+    cfg, a_pos, a_vel = dam_break_scene((128, 128, 128), (12.8, 12.8, 6.4), seed)
+    m = 0.025
+    bx = 12.8 - m - 127 * 0.05
+    b_pos, b_vel = generate_block((bx, m, m), (128, 128, 128), 0.05, 0.01 * 0.05, 1000.0 * 0.05 ** 3,
+                                  seed + 1)
+    return cfg, np.concatenate([a_pos, b_pos]), np.concatenate([a_vel, b_vel])
+
+
 # ------------------------------------------------------------ compiled reference
 def reference_available() -> bool:
     return reference() is not None

@@ -8,8 +8,9 @@ Two libraries come out of it:
   (MrMagne/position-based-fluids ``src/kernels/*.cl``) compiled as C++ through
   ``oracle/clshim.hpp`` and launched by ``oracle/ref_launch.cpp``.
 
-The reference sources are read where they lie, under ``/root/reference``; they
-are never copied into the repository.  The first stage runs the C++
+The reference sources are read where they lie: the checkout named by the
+environment variable ``PBF_REFERENCE_ROOT`` (default ``/root/reference``);
+they are never copied into the repository.  The first stage runs the C++
 preprocessor over each ``.cl`` file alone (comments dropped, the
 ``USE_LINKEDCELL`` branches of the active build resolved, no header expanded)
 and writes the kernel text to ``oracle/_ref/<kernel>.pre.cl``; the second
@@ -34,7 +35,10 @@ from pathlib import Path
 ORACLE_DIR = Path(__file__).resolve().parent
 BUILD_DIR = ORACLE_DIR / "_build"
 REF_DIR = ORACLE_DIR / "_ref"
-REFERENCE_KERNELS = Path("/root/reference/src/kernels")
+# The reference checkout: PBF_REFERENCE_ROOT, by default /root/reference.
+REFERENCE_ROOT = Path(os.environ.get("PBF_REFERENCE_ROOT", "/root/reference"))
+REFERENCE_KERNELS = REFERENCE_ROOT / "src" / "kernels"
+REFERENCE_SCENARIOS = REFERENCE_ROOT / "assets" / "scenarios"
 
 # The kernels of the reference's active (linked-cell) build, src/main.cpp:67-84.
 LIVE_KERNELS = [

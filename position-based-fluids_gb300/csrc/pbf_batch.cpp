@@ -66,6 +66,9 @@ struct pbf_batch {
   uint32_t n_total = 0, cells_total = 0;
   SortPlan plan;
   bool dirty = true;
+  // a step (or the tuner's trial steps) ran on the current layout, so the
+  // neighbour lists and counts belong to it
+  bool stepped_on_layout = false;
   cudaGraphExec_t graph = nullptr;
   bool graph_stale = false;
   std::vector<SceneDesc> table;
@@ -123,6 +126,7 @@ int apply_layout(pbf_batch *b) {
   }
   b->graph_stale = true;  // same kernels, new sizes: updated in place at the next step
   b->dirty = false;
+  b->stepped_on_layout = false;
   return PBF_OK;
 }
 
@@ -372,6 +376,7 @@ int pbf_batch_step(pbf_batch *b, uint32_t nsteps) {
     b->graph_stale = false;
   }
   for (uint32_t k = 0; k < nsteps; ++k) PBF_TRY(cudaGraphLaunch(b->graph, b->stream));
+  if (nsteps > 0) b->stepped_on_layout = true;
   return PBF_OK;
 }
 
@@ -446,7 +451,7 @@ int pbf_batch_launches_per_step(const pbf_batch *b, uint32_t *launches) {
 int pbf_batch_neighbour_stats(pbf_batch *b, uint32_t *max_count, uint32_t *overflow) {
   if (!b || !max_count || !overflow) return PBF_ERR_INVALID;
   // the lists belong to the current layout only after a step ran on it
-  if (!b->graph || b->graph_stale || b->dirty) return PBF_ERR_STATE;
+  if (b->dirty || !b->stepped_on_layout) return PBF_ERR_STATE;
   std::vector<uint32_t> cnt(b->n_total);
   if (b->n_total) {
     PBF_TRY(cudaMemcpyAsync(cnt.data(), b->d.nbr_cnt, (size_t)b->n_total * sizeof(uint32_t),
@@ -470,6 +475,7 @@ int pbf_batch_autotune(pbf_batch *b, uint32_t trial_steps, pbf_tuning *out) {
   if (b->n_total > 0) {
     PBF_TRY_STATUS(paper_autotune(b->d, b->n_total, b->stream, trial_steps,
                                   [&]() { return launch_batch_step(b); }, ms));
+    b->stepped_on_layout = true;  // the trial steps built lists on this layout
     if (b->graph) cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
     PBF_TRY_STATUS(pbf_batch_sync(b));

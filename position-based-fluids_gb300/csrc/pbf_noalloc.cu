@@ -37,11 +37,50 @@ constexpr size_t kNoAllocWords = words_for(kNoAllocMaxKeys);
 
 static __device__ __align__(256) uint32_t g_sort_scratch[kNoAllocWords];
 
+// The device address of g_sort_scratch is looked up once per CUDA context
+// (the host-side name is only a stand-in for it) and cached per device
+// ordinal together with the context's unique id.  A context created later on
+// the same device -- after cudaDeviceReset, or after the primary context was
+// released and retained again -- loads the module afresh, possibly at another
+// address; its different id makes the next call look the address up again.
+struct ScratchEntry {
+  unsigned long long ctx_id = 0;
+  void *address = nullptr;
+};
 std::mutex g_mutex;
-void *g_scratch_address[kMaxDevices] = {};
+ScratchEntry g_scratch[kMaxDevices];
 
-// Device address of g_sort_scratch on the current device, looked up once
-// per device (the host-side name is only a stand-in for it).
+using CtxGetCurrentFn = int (*)(void **);
+using CtxGetIdFn = int (*)(void *, unsigned long long *);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+std::once_flag g_entry_once;
+
+// Driver entry points (no link-time dependency on the driver library).
+void resolve_entry_points() {
+  void *fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) ==
+          cudaSuccess && q == cudaDriverEntryPointSuccess)
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
+  fn = nullptr;
+  if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) ==
+          cudaSuccess && q == cudaDriverEntryPointSuccess)
+    g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(fn);
+}
+
+// Unique id of the calling thread's current context, or 0 if none is current
+// (or the driver cannot tell).
+unsigned long long current_context_id() {
+  std::call_once(g_entry_once, resolve_entry_points);
+  if (!g_ctx_get_current || !g_ctx_get_id) return 0;
+  void *ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != 0 || !ctx) return 0;
+  unsigned long long id = 0;
+  return g_ctx_get_id(ctx, &id) == 0 ? id : 0;
+}
+
+// Device address of g_sort_scratch in the current device's context.
 int scratch_address(uint32_t **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -51,13 +90,16 @@ int scratch_address(uint32_t **out) {
     return PBF_ERR_INVALID;
   }
   std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_scratch_address[dev]) {
+  ScratchEntry &entry = g_scratch[dev];
+  const unsigned long long id = current_context_id();
+  if (!entry.address || id == 0 || id != entry.ctx_id) {
     void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_sort_scratch);
+    e = cudaGetSymbolAddress(&p, g_sort_scratch);  // makes the primary context current
     if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress");
-    g_scratch_address[dev] = p;
+    entry.address = p;
+    entry.ctx_id = current_context_id();
   }
-  *out = static_cast<uint32_t *>(g_scratch_address[dev]);
+  *out = static_cast<uint32_t *>(entry.address);
   return PBF_OK;
 }
 

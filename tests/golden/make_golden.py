@@ -14,7 +14,7 @@ layout), predicted positions (.w = density of the last lambda pass), lambda
 of the last iteration, and the cell of every particle as recorded in the
 reference's linked cell lists of the last step.
 
-Usage (in a checkout next to the reference tree):
+Usage (the reference checkout in PBF_REFERENCE_ROOT, see oracle/build.py):
     python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -29,7 +29,7 @@ sys.path.insert(0, str(ROOT))
 
 import oracle  # noqa: E402
 
-SCENARIOS = Path("/root/reference/assets/scenarios")
+from oracle.build import REFERENCE_SCENARIOS as SCENARIOS  # noqa: E402  (PBF_REFERENCE_ROOT)
 OUT = Path(__file__).resolve().parent / "ref_scenarios.npz"
 
 # name -> step counts.  box.in goes non-finite in the reference's own

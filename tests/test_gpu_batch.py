@@ -97,8 +97,14 @@ def test_batch_neighbour_stats_match_the_plain_simulations(pbf):
             with pytest.raises(pbf.PbfError) as e:
                 b.neighbour_stats()
             assert e.value.status == pbf.ERR_STATE
+            b.step(0)  # applies the layout and captures the step, steps nothing
+            with pytest.raises(pbf.PbfError) as e:
+                b.neighbour_stats()
+            assert e.value.status == pbf.ERR_STATE
             b.step(5)
             mx, over = b.neighbour_stats()
+            b.set_tuning(b.tuning())  # a new launch shape keeps the lists
+            assert b.neighbour_stats() == (mx, over)
         assert mx == max(m for m, _ in alone)
         assert over == sum(o for _, o in alone)
         assert (over > 0) == (cap == 16)

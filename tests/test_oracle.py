@@ -39,9 +39,8 @@ def test_restatement_matches_golden_bit_for_bit(golden, oracle_mod):
 def test_restatement_matches_live_reference(oracle_mod):
     if not oracle_mod.reference_available():
         pytest.skip("the reference's kernels are not buildable on this host")
-    from pathlib import Path
+    from oracle.build import REFERENCE_SCENARIOS as scen
 
-    scen = Path("/root/reference/assets/scenarios")
     if not scen.is_dir():
         pytest.skip("reference scenarios not present")
     for name, steps in [("dam2", 3), ("drop", 3), ("dam_coarse", 3), ("dam_miles", 10), ("box_big", 10)]:
@@ -244,3 +243,28 @@ def test_paper_oracle_conserves_momentum_without_walls(oracle_mod):
     # XSPH and vorticity terms conserve momentum only approximately (1/rho_j
     # weights); velocities stay finite and small.
     assert np.abs(ovel[:, :3]).max() < 10.0
+
+
+def test_oracle_scenes_match_the_library_generator(oracle_mod):
+    """The oracle builds the benchmark scenes itself (so that the CPU run of
+    the reference's kernels loads nothing of the product); its generator
+    equals pbf_generate_block bit for bit."""
+    import __graft_entry__ as ge
+
+    pbf = ge.load_package()
+    for dims, seed in [((3, 4, 5), 7), ((16, 8, 4), 0x5EED), ((1, 1, 1), 2**64 - 1)]:
+        ps = pbf.scenes.block((0.025, 0.025, 0.025), dims, seed)
+        want_pos, want_vel = pbf.state_from_particles(ps)
+        pos, vel = oracle_mod.generate_block((0.025, 0.025, 0.025), dims, 0.05, 0.0005, 0.125, seed)
+        assert np.array_equal(bits(pos), bits(want_pos)), dims
+        assert np.array_equal(bits(vel), bits(want_vel)), dims
+    cfg, pos, vel = oracle_mod.scene_1m()
+    sc = pbf.scenes.config_1m()
+    want_pos, want_vel = pbf.state_from_particles(sc.particles)
+    assert np.array_equal(bits(pos), bits(want_pos))
+    assert np.array_equal(bits(vel), bits(want_vel))
+    p = sc.params
+    for f, g in [("x_min", "x_min"), ("x_max", "x_max"), ("y_max", "y_max"), ("z_max", "z_max"),
+                 ("x_n", "x_n"), ("y_n", "y_n"), ("z_n", "z_n"),
+                 ("timestep_length", "time_step_length"), ("rest_density", "rest_density")]:
+        assert np.float32(getattr(cfg, f)) == np.float32(getattr(p, g)), f

@@ -29,13 +29,14 @@ def _sort_with_scratch(lib, keys, vals, bits, stream):
     return ko, vo
 
 
-def _sort_noalloc(lib, keys, vals, bits, stream):
+def _sort_noalloc(lib, keys, vals, bits, stream, with_status=True):
     n = keys.shape[0]
     ko = torch.empty(n, dtype=torch.int32, device="cuda")
     vo = torch.empty(n, dtype=torch.int32, device="cuda")
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
     assert lib.pbf_op_sort_pairs_noalloc(keys.data_ptr(), vals.data_ptr() if vals is not None else None, n,
-                                         bits, ko.data_ptr(), vo.data_ptr(), status.data_ptr(), stream) == 0
+                                         bits, ko.data_ptr(), vo.data_ptr(),
+                                         status.data_ptr() if with_status else None, stream) == 0
     return ko, vo, status
 
 
@@ -43,13 +44,18 @@ def test_noalloc_sort_matches_scratch_sort_twice(pbf):
     lib = pbf.lib()
     stream = torch.cuda.current_stream().cuda_stream
     rng = np.random.default_rng(2024)
-    cases = [(1 << 20, 18, None), (333_333, 13, "vals")]
-    for n, bits, with_vals in cases:
-        keys = torch.from_numpy(rng.integers(0, 1 << bits, n).astype(np.int32)).cuda()
+    # (n, key bits, explicit values, status word): 32-bit keys take four
+    # digit passes, the largest scratch layout, at the maximum size; one
+    # case leaves the status pointer NULL
+    cases = [(1 << 20, 18, None, True), (333_333, 13, "vals", True), (1 << 20, 32, "vals", True),
+             (1 << 20, 32, None, False)]
+    for n, bits, with_vals, with_status in cases:
+        keys = torch.from_numpy(rng.integers(0, 1 << bits, n, dtype=np.uint64).astype(np.uint32)
+                                .view(np.int32)).cuda()
         vals = (torch.from_numpy(rng.integers(0, 1 << 30, n).astype(np.int32)).cuda()
                 if with_vals else None)
         want_k, want_v = _sort_with_scratch(lib, keys, vals, bits, stream)
-        got_k, got_v, status = _sort_noalloc(lib, keys, vals, bits, stream)
+        got_k, got_v, status = _sort_noalloc(lib, keys, vals, bits, stream, with_status)
         torch.cuda.synchronize()
         assert int(status.item()) == 0
         assert torch.equal(got_k, want_k) and torch.equal(got_v, want_v)
