@@ -222,13 +222,18 @@ int pbf_launches_per_step(const pbf_sim *sim, uint32_t *launches);
  * lambda, 3 delta-p, 4 vorticity, 5 XSPH + commit.  threads = 64, 128 or
  * 256 per CTA; batch = 4 or 8 neighbour loads in flight per thread (ignored
  * for 0 and 1); fuse_first = 1 runs 1 instead of 0 + 2 for the first solver
- * iteration.  No shape changes a result bit.  trial_ms is the tuner's best
- * time per launch of each pass (0 when untuned). */
+ * iteration.  staged = 1 runs every gather pass on staged tiles instead: a
+ * CTA per 128 sorted slots copies its neighbourhood into shared memory with
+ * bulk asynchronous copies and the passes read neighbours from there
+ * (threads, batch and fuse_first then do not apply).  No shape changes a
+ * result bit.  trial_ms is the tuner's best time per launch of each pass (0
+ * when untuned). */
 typedef struct pbf_tuning {
   uint32_t threads[6];
   uint32_t batch[6];
   uint32_t fuse_first;
   float trial_ms[6];
+  uint32_t staged;
 } pbf_tuning;
 /* Times every shape over `trial_steps` steps (1..32) of this simulation
  * from its current state, keeps the fastest per pass and restores the state
@@ -249,6 +254,13 @@ int pbf_get_density(pbf_sim *sim, float *density);
  * as a listed set; a nonzero *overflow says the capacity is too small for
  * the scene.  PBF_ERR_STATE in REF_COMPAT mode or before the first step. */
 int pbf_neighbour_stats(pbf_sim *sim, uint32_t *max_count, uint32_t *overflow);
+/* Staged tiles of the last step (PAPER mode with staged = 1 in the
+ * tuning): how many 128-slot tiles staged their neighbourhood in shared
+ * memory and how many gathered through L1 instead (more than three grid
+ * rows in the tile, or more than 2048 candidates).  Both 0 when the last
+ * step ran the L1 passes.  PBF_ERR_STATE in REF_COMPAT mode or before the
+ * first step.  No reference counterpart. */
+int pbf_tile_stats(pbf_sim *sim, uint32_t *staged, uint32_t *unstaged);
 /* The neighbour structure the last step built, in input particle order:
  * hash[i] = cell of particle i; perm[q] = input index of the particle at
  * sorted position q (ties by input index in REF_COMPAT mode, by previous

@@ -113,11 +113,12 @@ class Tuning(C.Structure):
 
     PASSES = ("nbr_build", "nbr_lambda", "lambda", "delta", "vorticity", "xsph_commit")
     _fields_ = [("threads", C.c_uint32 * 6), ("batch", C.c_uint32 * 6), ("fuse_first", C.c_uint32),
-                ("trial_ms", C.c_float * 6)]
+                ("trial_ms", C.c_float * 6), ("staged", C.c_uint32)]
 
     def as_dict(self) -> dict:
         return {"threads": dict(zip(self.PASSES, self.threads)), "batch": dict(zip(self.PASSES, self.batch)),
-                "fuse_first": int(self.fuse_first), "trial_ms": dict(zip(self.PASSES, self.trial_ms))}
+                "fuse_first": int(self.fuse_first), "staged": int(self.staged),
+                "trial_ms": dict(zip(self.PASSES, self.trial_ms))}
 
 
 class ServerStats(C.Structure):
@@ -193,6 +194,7 @@ def lib():
             "pbf_launches_per_step": ([vp, C.POINTER(u32)], i32),
             "pbf_get_density": ([vp, vp], i32),
             "pbf_neighbour_stats": ([vp, C.POINTER(u32), C.POINTER(u32)], i32),
+            "pbf_tile_stats": ([vp, C.POINTER(u32), C.POINTER(u32)], i32),
             "pbf_get_cells": ([vp, vp, vp, vp], i32),
             "pbf_destroy": ([vp], i32),
             "pbf_autotune": ([vp, u32, C.POINTER(Tuning)], i32),
@@ -425,6 +427,12 @@ class Simulation:
         mx, over = C.c_uint32(), C.c_uint32()
         _check(lib().pbf_neighbour_stats(self._h, C.byref(mx), C.byref(over)), "pbf_neighbour_stats")
         return mx.value, over.value
+
+    def tile_stats(self) -> tuple[int, int]:
+        """(staged, unstaged) 128-slot tiles of the last step's staged passes."""
+        a, b = C.c_uint32(), C.c_uint32()
+        _check(lib().pbf_tile_stats(self._h, C.byref(a), C.byref(b)), "pbf_tile_stats")
+        return int(a.value), int(b.value)
 
     def cells(self):
         """(hash per particle, sorted permutation, inclusive ranges per cell)."""

@@ -34,11 +34,12 @@ NO_FMAD = {"pbf_refcompat.cu"}
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
              "-Wno-unused-parameter", "-I", str(CUDA_HOME / "include"), "-I", str(REPO / "include")]
 
-CU_SOURCES = ["pbf_sort.cu", "pbf_paper.cu", "pbf_refcompat.cu", "pbf_noalloc.cu", "pbf_render.cu"]
+CU_SOURCES = ["pbf_sort.cu", "pbf_paper.cu", "pbf_tile.cu", "pbf_refcompat.cu", "pbf_noalloc.cu",
+              "pbf_render.cu"]
 CPP_SOURCES = ["pbf_params.cpp", "pbf_scenario.cpp", "pbf_sim.cpp", "pbf_batch.cpp", "pbf_server.cpp",
                "Simulation.cpp"]
 RUNNER_SOURCES = ["pbf_run.cpp"]
-HEADERS = ["pbf_internal.cuh", "pbf_device.cuh", "pbf_host.hpp", "Simulation.hpp"]
+HEADERS = ["pbf_internal.cuh", "pbf_device.cuh", "pbf_paper.cuh", "pbf_host.hpp", "Simulation.hpp"]
 
 
 def _run(cmd: list[str]) -> str:

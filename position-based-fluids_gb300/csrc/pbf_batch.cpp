@@ -48,7 +48,8 @@ size_t bytes_per_particle(uint32_t maxn) {
          + sizeof(float)                      // R
          + (size_t)paper_list_words(maxn) * 16  // lists
          + sizeof(uint16_t)                   // sid
-         + 2 * sizeof(float4);                // io staging
+         + 2 * sizeof(float4)                 // io staging
+         + (4 + kTileSegs * 8 + kTileSlots - 1) / kTileSlots;  // tile plan
 }
 
 }  // namespace
@@ -143,6 +144,17 @@ int launch_batch_step(pbf_batch *b) {
   PBF_TRY(cell_offsets_runs(d.skeys, n, b->cells_total, d.offsets, d.runs, d.runs_count, st));
   PBF_TRY(paper_reorder(d.perm, d.X, d.V, d.ID, n, pc, d.X2, d.V2, d.ID2, d.P, d.D, st));
   const uint32_t iters = b->solver.solver_iterations;
+  if (d.tune.staged) {
+    PBF_TRY(tile_plan(d, pc, d.sid, st));
+    for (uint32_t it = 0; it < iters; ++it) {
+      if (it == 0) PBF_TRY(tile_nbr_build(d, pc, d.sid, st));
+      PBF_TRY(tile_lambda(d, pc, d.sid, st));
+      PBF_TRY(tile_delta(d, pc, d.sid, it + 1 == iters, st));
+    }
+    PBF_TRY(tile_vorticity(d, pc, d.sid, st));
+    PBF_TRY(tile_xsph_commit(d, pc, d.sid, st));
+    return PBF_OK;
+  }
   for (uint32_t it = 0; it < iters; ++it) {
     if (it == 0 && d.tune.fuse_first) {
       PBF_TRY(paper_nbr_lambda(d, pc, d.sid, st));
@@ -251,6 +263,9 @@ int pbf_batch_create(const pbf_params *solver, uint32_t max_scenes, uint32_t max
   A(&d.ID, M); A(&d.ID2, M); A(&d.keys, M); A(&d.skeys, M); A(&d.perm, M);
   A(&d.nbr_cnt, M); A(&d.R, M); A(&d.sid, M);
   A(&d.nbr, (size_t)paper_list_words(b->pc.maxn) * M);
+  A(&d.tile_info, tile_count(max_particles));
+  A(&d.tile_seg, (size_t)tile_count(max_particles) * kTileSegs);
+  A(&d.tile_stats, 2);
   A(&d.io_pos, M); A(&d.io_vel, M);
   A(&d.offsets, (size_t)max_cells + 1);
   A(&d.runs, offset_runs_capacity(max_cells));
@@ -258,6 +273,10 @@ int pbf_batch_create(const pbf_params *solver, uint32_t max_scenes, uint32_t max
   A(&d.sort_scratch, make_sort_plan(max_particles, 32).words);
   A(&d.scenes, max_scenes);
   A(&d.err, 1);
+  if (rc == PBF_OK) {
+    const cudaError_t te = tile_init();
+    if (te != cudaSuccess) rc = cuda_status(te, "tile_init");
+  }
   if (rc != PBF_OK) {
     release(b.get());
     return rc;

@@ -14,6 +14,7 @@ namespace pbf {
 // host reads back at synchronisation points.
 enum DeviceError : uint32_t {
   kDevErrLookback = 1u,  // a radix-sort look-back wait hit its bound
+  kDevErrStage = 2u,     // a tile's bulk copies did not complete within the bounded wait
 };
 
 // ------------------------------------------------------------ grid / scene --
@@ -143,6 +144,9 @@ struct GatherTuning {
   uint8_t block[kGatherKinds] = {1, 1, 2, 1, 2, 1};
   uint8_t batch[kGatherKinds] = {0, 0, 0, 0, 0, 0};  // neighbour loads in flight: 4 << code
   uint8_t fuse_first = 0;  // 1: one kernel builds the lists and computes the first lambda
+  // 1: the gather passes stage each tile's neighbourhood in shared memory
+  // (pbf_tile.cu; one 128-thread shape, fuse_first does not apply)
+  uint8_t staged = 0;
 };
 constexpr int kBlockCodes = 3;  // 64, 128, 256
 constexpr int kBatchCodes = 2;  // 4, 8
@@ -216,12 +220,16 @@ struct DeviceState {
   uint32_t *offsets = nullptr;         // ncells + 1
   uint4 *runs = nullptr;               // offset_runs_capacity(ncells) queued runs
   uint32_t *runs_count = nullptr;
-  uint4 *nbr = nullptr;                // neighbour lists, 4 slots per word (paper)
+  uint4 *nbr = nullptr;                // neighbour lists, 4 slots or 8 staged indices per word (paper)
   uint32_t *nbr_cnt = nullptr;         // neighbour counts (paper)
   uint32_t *sort_scratch = nullptr;
   uint32_t *err = nullptr;             // device error flag word
   SceneDesc *scenes = nullptr;         // device scene table
   float4 *io_pos = nullptr, *io_vel = nullptr; // input-order staging
+  // staged tiles (paper): per tile of kTileSlots slots its plan
+  uint32_t *tile_info = nullptr;       // pieces and their first slots (0: not staged)
+  uint2 *tile_seg = nullptr;           // kTileSegs (first slot, length) per tile
+  uint32_t *tile_stats = nullptr;      // staged and unstaged tiles of the last plan
   // batches only (null for a single scene)
   uint16_t *sid = nullptr;             // scene of each sorted slot
   // host-side launch shape of the gather passes, and the tuner's timer
@@ -234,6 +242,30 @@ cudaError_t scene_ids(const SceneDesc *scenes, uint32_t nscenes, uint32_t n, uin
                       cudaStream_t st);
 // dst[i] = i for i in [0, n).
 cudaError_t iota_range(uint32_t *dst, uint32_t n, cudaStream_t st);
+
+// ------------------------------------------------------------ staged tiles
+// Sorted slots per tile of the staged gather passes (= threads per CTA), and
+// segment-table entries per tile (9 per grid row, at most three rows).
+constexpr uint32_t kTileSlots = 128;
+constexpr uint32_t kTileSegs = 32;
+uint32_t tile_count(uint32_t n);
+// Sets the kernels' shared-memory limits (once per process); the launches
+// below call it too.
+cudaError_t tile_init();
+// The step's tile plan (after the cell offsets), then the staged passes:
+// the same outputs as the paper_* launches of the same names.
+cudaError_t tile_plan(const DeviceState &d, const PaperConsts &c, const uint16_t *sid,
+                      cudaStream_t st);
+cudaError_t tile_nbr_build(const DeviceState &d, const PaperConsts &c, const uint16_t *sid,
+                           cudaStream_t st);
+cudaError_t tile_lambda(const DeviceState &d, const PaperConsts &c, const uint16_t *sid,
+                        cudaStream_t st);
+cudaError_t tile_delta(const DeviceState &d, const PaperConsts &c, const uint16_t *sid, bool last,
+                       cudaStream_t st);
+cudaError_t tile_vorticity(const DeviceState &d, const PaperConsts &c, const uint16_t *sid,
+                           cudaStream_t st);
+cudaError_t tile_xsph_commit(const DeviceState &d, const PaperConsts &c, const uint16_t *sid,
+                             cudaStream_t st);
 
 // ------------------------------------------------------- paper-mode launches
 // 16-byte list words per particle for a list capacity of maxn neighbours.
@@ -256,7 +288,7 @@ cudaError_t paper_nbr_lambda(const DeviceState &d, const PaperConsts &c,
 // Launches of the first solver iteration's list build and lambda pass under
 // the current tuning (1 fused or 2).
 inline uint32_t paper_first_launches(const DeviceState &d) {
-  return d.tune.fuse_first ? 1u : 2u;
+  return d.tune.staged ? 3u /*plan, build, lambda*/ : (d.tune.fuse_first ? 1u : 2u);
 }
 cudaError_t paper_lambda(const DeviceState &d, const PaperConsts &c,
                          const uint16_t *sid, cudaStream_t st);

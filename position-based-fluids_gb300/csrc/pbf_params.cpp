@@ -238,6 +238,7 @@ void to_pbf_tuning(const GatherTuning &g, const double trial_ms[kGatherKinds], p
     out->trial_ms[k] = trial_ms ? (float)trial_ms[k] : 0.0f;
   }
   out->fuse_first = g.fuse_first;
+  out->staged = g.staged;
 }
 
 int to_gather_tuning(const pbf_tuning &t, GatherTuning *out) {
@@ -260,6 +261,11 @@ int to_gather_tuning(const pbf_tuning &t, GatherTuning *out) {
     return PBF_ERR_INVALID;
   }
   g.fuse_first = (uint8_t)t.fuse_first;
+  if (t.staged > 1) {
+    set_error_message("tuning: staged must be 0 or 1");
+    return PBF_ERR_INVALID;
+  }
+  g.staged = (uint8_t)t.staged;
   *out = g;
   return PBF_OK;
 }

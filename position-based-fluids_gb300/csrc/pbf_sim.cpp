@@ -155,25 +155,44 @@ int launch_step(pbf_sim *s) {
                           d.P, d.D, st));
     PBF_TRY_STATUS(mark(s, 0, "reorder", 1, &ev));
     const uint32_t iters = s->prm.solver_iterations;
-    for (uint32_t it = 0; it < iters; ++it) {
-      if (it == 0 && d.tune.fuse_first) {
-        PBF_TRY(paper_nbr_lambda(d, s->pc, nullptr, st));
-        PBF_TRY_STATUS(mark(s, 1, "nbr_lambda", 1, &ev));
-      } else {
+    if (d.tune.staged) {
+      PBF_TRY(tile_plan(d, s->pc, nullptr, st));
+      PBF_TRY_STATUS(mark(s, 0, "tile_plan", 1, &ev));
+      for (uint32_t it = 0; it < iters; ++it) {
         if (it == 0) {
-          PBF_TRY(paper_nbr_build(d, s->pc, nullptr, st));
+          PBF_TRY(tile_nbr_build(d, s->pc, nullptr, st));
           PBF_TRY_STATUS(mark(s, 1, "nbr_build", 1, &ev));
         }
-        PBF_TRY(paper_lambda(d, s->pc, nullptr, st));
+        PBF_TRY(tile_lambda(d, s->pc, nullptr, st));
         PBF_TRY_STATUS(mark(s, 1, "lambda", 1, &ev));
+        PBF_TRY(tile_delta(d, s->pc, nullptr, it + 1 == iters, st));
+        PBF_TRY_STATUS(mark(s, 2, "delta", 1, &ev));
       }
-      PBF_TRY(paper_delta(d, s->pc, nullptr, it + 1 == iters, st));
-      PBF_TRY_STATUS(mark(s, 2, "delta", 1, &ev));
+      PBF_TRY(tile_vorticity(d, s->pc, nullptr, st));
+      PBF_TRY_STATUS(mark(s, 3, "vorticity", 1, &ev));
+      PBF_TRY(tile_xsph_commit(d, s->pc, nullptr, st));
+      PBF_TRY_STATUS(mark(s, 3, "xsph_commit", 1, &ev));
+    } else {
+      for (uint32_t it = 0; it < iters; ++it) {
+        if (it == 0 && d.tune.fuse_first) {
+          PBF_TRY(paper_nbr_lambda(d, s->pc, nullptr, st));
+          PBF_TRY_STATUS(mark(s, 1, "nbr_lambda", 1, &ev));
+        } else {
+          if (it == 0) {
+            PBF_TRY(paper_nbr_build(d, s->pc, nullptr, st));
+            PBF_TRY_STATUS(mark(s, 1, "nbr_build", 1, &ev));
+          }
+          PBF_TRY(paper_lambda(d, s->pc, nullptr, st));
+          PBF_TRY_STATUS(mark(s, 1, "lambda", 1, &ev));
+        }
+        PBF_TRY(paper_delta(d, s->pc, nullptr, it + 1 == iters, st));
+        PBF_TRY_STATUS(mark(s, 2, "delta", 1, &ev));
+      }
+      PBF_TRY(paper_vorticity(d, s->pc, nullptr, st));
+      PBF_TRY_STATUS(mark(s, 3, "vorticity", 1, &ev));
+      PBF_TRY(paper_xsph_commit(d, s->pc, nullptr, st));
+      PBF_TRY_STATUS(mark(s, 3, "xsph_commit", 1, &ev));
     }
-    PBF_TRY(paper_vorticity(d, s->pc, nullptr, st));
-    PBF_TRY_STATUS(mark(s, 3, "vorticity", 1, &ev));
-    PBF_TRY(paper_xsph_commit(d, s->pc, nullptr, st));
-    PBF_TRY_STATUS(mark(s, 3, "xsph_commit", 1, &ev));
   } else {
     PBF_TRY(rc_predict_hash(d.X, d.V, d.P, n, s->rc, d.scenes, d.keys, s->plan,
                             d.sort_scratch, st));
@@ -336,12 +355,19 @@ int pbf_init(pbf_sim *s) {
     A(&d.R, n);
     A(&d.nbr_cnt, n);
     A(&d.nbr, (size_t)paper_list_words(s->pc.maxn) * n);
+    A(&d.tile_info, tile_count(s->n));
+    A(&d.tile_seg, (size_t)tile_count(s->n) * kTileSegs);
+    A(&d.tile_stats, 2);
   } else {
     A(&d.PS, n);
     A(&d.PS2, n);
     A(&d.VS, n);
     A(&d.DV, n);
     A(&d.SS, n);
+  }
+  if (rc == PBF_OK && s->paper) {
+    const cudaError_t te = tile_init();
+    if (te != cudaSuccess) rc = cuda_status(te, "tile_init");
   }
   if (rc != PBF_OK) {
     free_all(s);
@@ -609,6 +635,19 @@ int pbf_neighbour_stats(pbf_sim *s, uint32_t *max_count, uint32_t *overflow) {
   }
   *max_count = mx;
   *overflow = over;
+  return PBF_OK;
+}
+
+int pbf_tile_stats(pbf_sim *s, uint32_t *staged, uint32_t *unstaged) {
+  if (!ready(s) || !staged || !unstaged) return ready(s) ? PBF_ERR_INVALID : PBF_ERR_STATE;
+  if (!s->paper || !s->stepped) return PBF_ERR_STATE;
+  uint32_t st[2] = {0u, 0u};
+  if (s->d.tune.staged) {
+    PBF_TRY(cudaMemcpyAsync(st, s->d.tile_stats, sizeof st, cudaMemcpyDeviceToHost, s->stream));
+    PBF_TRY(cudaStreamSynchronize(s->stream));
+  }
+  *staged = st[0];
+  *unstaged = st[1];
   return PBF_OK;
 }
 

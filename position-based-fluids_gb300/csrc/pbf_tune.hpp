@@ -14,7 +14,9 @@ namespace pbf {
 // Times every launch shape (threads per CTA x neighbour loads in flight x
 // list build fused with the first lambda or not) over `trials` steps, each
 // shape from the same state, and keeps for every gather pass the shape with
-// the shortest launches.  The current shapes are timed first and a pass
+// the shortest launches.  Then it times whole steps of that choice against
+// the staged tiles (pbf_tile.cu) from the same state and keeps the staged
+// passes when their steps are more than kTuneMargin faster.  The current shapes are timed first and a pass
 // moves to another shape only when that one is more than kTuneMargin
 // faster: on a near-tie the pick would follow timing noise, and the
 // defaults are the shapes measured fastest over a whole dam break, where
@@ -61,6 +63,7 @@ int paper_autotune(DeviceState &d, uint32_t n, cudaStream_t st, uint32_t trials,
   };
   const GatherTuning before = d.tune;
   GatherTuning best = before;
+  best.staged = 0;
   double best_ms[kGatherKinds];
   for (int k = 0; k < kGatherKinds; ++k) best_ms[k] = std::numeric_limits<double>::infinity();
   // Runs `trials` steps (one, untimed, when !timed) with shapes t from the
@@ -100,6 +103,7 @@ int paper_autotune(DeviceState &d, uint32_t n, cudaStream_t st, uint32_t trials,
       const bool timed = pass == 1;
       if (timed) {
         GatherTuning cur = before;
+        cur.staged = 0;
         for (int fuse = 0; fuse < 2 && rc == PBF_OK; ++fuse) {
           cur.fuse_first = (uint8_t)fuse;
           if (!trial(cur, true, true)) break;
@@ -113,9 +117,33 @@ int paper_autotune(DeviceState &d, uint32_t n, cudaStream_t st, uint32_t trials,
     if (rc == PBF_OK) {
       best.fuse_first =
           best_ms[kKindNbrLambda] < best_ms[kKindNbr] + best_ms[kKindLambda] ? 1u : 0u;
+      best.staged = 0;
       for (int k = 0; k < kGatherKinds; ++k)
         per_launch_ms[k] = best_ms[k] < std::numeric_limits<double>::infinity() ? best_ms[k] : 0.0;
     }
+    // whole steps: the L1-gather choice against the staged tiles
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (rc == PBF_OK && cuda(cudaEventCreate(&e0), "tune events") &&
+        cuda(cudaEventCreate(&e1), "tune events")) {
+      GatherTuning staged = best;
+      staged.staged = 1;
+      float step_ms[2] = {0.f, 0.f};
+      for (int v = 0; v < 2 && rc == PBF_OK; ++v) {
+        const GatherTuning &t = v == 0 ? best : staged;
+        if (!trial(t, false, false)) break;  // loads the variant's kernels
+        if (!copy_state(false)) break;
+        d.tune = t;
+        if (!cuda(cudaEventRecord(e0, st), "tune timing")) break;
+        for (uint32_t i = 0; i < trials && rc == PBF_OK; ++i) rc = step();
+        if (rc != PBF_OK || !cuda(cudaEventRecord(e1, st), "tune timing") ||
+            !cuda(cudaEventSynchronize(e1), "tune timing") ||
+            !cuda(cudaEventElapsedTime(&step_ms[v], e0, e1), "tune timing"))
+          break;
+      }
+      if (rc == PBF_OK && step_ms[1] < step_ms[0] * (1.0 - kTuneMargin)) best = staged;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
     copy_state(false);
     cuda(cudaStreamSynchronize(st), "tune sync");
   }
