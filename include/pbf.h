@@ -100,6 +100,9 @@ typedef struct {
   float gravity_y;                /* [gravity_y] paper mode               */
   float wall_margin;              /* [wall_margin] paper mode, in metres  */
   uint32_t max_neighbours;        /* [max_neighbours] stored per particle */
+  uint32_t grow_lists;            /* [grow_lists] 1: a simulation's list  */
+                                  /* capacity grows with its scene (see   */
+                                  /* pbf_list_capacity); 0: fixed         */
 } pbf_params;
 
 /* Particle (src/Particle.hpp:9-14): mass, position, velocity, acceleration
@@ -119,7 +122,8 @@ const char *pbf_last_error_message(void);
 
 /* Defaults: mode PAPER, 4 iterations, relax_eps 600, s_corr k 0.1 n 4
  * dq 0.2, XSPH c 0.01, vorticity eps 0.0005, gravity -9.81, wall margin
- * h/4 (resolved at create time when negative), max_neighbours 128. */
+ * h/4 (resolved at create time when negative), max_neighbours 128,
+ * grow_lists 1. */
 void pbf_params_default(pbf_params *p);
 
 /* ------------------------------------------------ scenario layer (L0) */
@@ -254,6 +258,17 @@ int pbf_get_density(pbf_sim *sim, float *density);
  * as a listed set; a nonzero *overflow says the capacity is too small for
  * the scene.  PBF_ERR_STATE in REF_COMPAT mode or before the first step. */
 int pbf_neighbour_stats(pbf_sim *sim, uint32_t *max_count, uint32_t *overflow);
+/* Neighbour-list capacity (entries per particle) the simulation uses now,
+ * and how many times it has grown.  It starts at max_neighbours rounded down
+ * to a multiple of 8 and grows by itself: each step records its largest
+ * neighbour count, and when that comes within 1/8 of the capacity the lists
+ * are reallocated to 1.5x the count (at most 1024) before the next step is
+ * launched, unless pbf_params.grow_lists is 0.  (Batches and servers keep
+ * the capacity they were created with.)  (pbf_step therefore keeps at most two steps queued: before
+ * launching a step it waits for the step two back -- the first step's
+ * count right after that step -- while the step before still runs.)  No
+ * reference counterpart; grows may be NULL. */
+int pbf_list_capacity(const pbf_sim *sim, uint32_t *capacity, uint32_t *grows);
 /* Staged tiles of the last step (PAPER mode with staged = 1 in the
  * tuning): how many 128-slot tiles staged their neighbourhood in shared
  * memory and how many gathered through L1 instead (more than three grid

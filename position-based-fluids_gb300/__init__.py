@@ -72,6 +72,7 @@ class Params(C.Structure):
         ("gravity_y", C.c_float),
         ("wall_margin", C.c_float),
         ("max_neighbours", C.c_uint32),
+        ("grow_lists", C.c_uint32),
     ]
 
     @property
@@ -195,6 +196,7 @@ def lib():
             "pbf_get_density": ([vp, vp], i32),
             "pbf_neighbour_stats": ([vp, C.POINTER(u32), C.POINTER(u32)], i32),
             "pbf_tile_stats": ([vp, C.POINTER(u32), C.POINTER(u32)], i32),
+            "pbf_list_capacity": ([vp, C.POINTER(u32), C.POINTER(u32)], i32),
             "pbf_get_cells": ([vp, vp, vp, vp], i32),
             "pbf_destroy": ([vp], i32),
             "pbf_autotune": ([vp, u32, C.POINTER(Tuning)], i32),
@@ -427,6 +429,12 @@ class Simulation:
         mx, over = C.c_uint32(), C.c_uint32()
         _check(lib().pbf_neighbour_stats(self._h, C.byref(mx), C.byref(over)), "pbf_neighbour_stats")
         return mx.value, over.value
+
+    def list_capacity(self) -> tuple[int, int]:
+        """(neighbour-list capacity in use, times it has grown)."""
+        cap, grows = C.c_uint32(), C.c_uint32()
+        _check(lib().pbf_list_capacity(self._h, C.byref(cap), C.byref(grows)), "pbf_list_capacity")
+        return int(cap.value), int(grows.value)
 
     def tile_stats(self) -> tuple[int, int]:
         """(staged, unstaged) 128-slot tiles of the last step's staged passes."""

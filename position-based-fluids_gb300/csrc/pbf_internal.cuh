@@ -222,6 +222,7 @@ struct DeviceState {
   uint32_t *runs_count = nullptr;
   uint4 *nbr = nullptr;                // neighbour lists, 4 slots or 8 staged indices per word (paper)
   uint32_t *nbr_cnt = nullptr;         // neighbour counts (paper)
+  uint32_t *nbr_max = nullptr;         // largest neighbour count of the step (paper)
   uint32_t *sort_scratch = nullptr;
   uint32_t *err = nullptr;             // device error flag word
   SceneDesc *scenes = nullptr;         // device scene table

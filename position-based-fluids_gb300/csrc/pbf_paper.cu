@@ -127,12 +127,13 @@ __global__ void __launch_bounds__(kBlock)
   const size_t stride = 4ull * c.n;  // words from one list group to the next
   uint32_t cnt = 0;
   scan_members(pk, nc.skeys[k], scene_of(nc.scenes, nc.sid, k), nc.off, P, c,
-               [&](uint32_t j, float, float, float, float) {
+               [&](uint32_t j, const Sep &) {
                  if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j;
                  ++cnt;
                });
   pad_list(out, stride, cnt, c.maxn, k);
   nbr_cnt[k] = cnt;
+  record_count(nc.cnt_max, cnt);
 }
 
 // k_nbr_build fused with the first lambda pass: the same lists, and lambda
@@ -153,13 +154,14 @@ __global__ void __launch_bounds__(kBlock)
   uint32_t cnt = 0;
   LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
   scan_members(pk, nc.skeys[k], scene_of(nc.scenes, nc.sid, k), nc.off, P, c,
-               [&](uint32_t j, float rx, float ry, float rz, float r2) {
+               [&](uint32_t j, const Sep &r) {
                  if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j;
                  ++cnt;
-                 acc.add(rx, ry, rz, r2, c);
+                 acc.add(r, c);
                });
   pad_list(out, stride, cnt, c.maxn, k);
   nbr_cnt[k] = cnt;
+  record_count(nc.cnt_max, cnt);
   Q[k] = make_float4(pk.x, pk.y, pk.z, acc.lambda(c));
   R[k] = acc.rho;
 }
@@ -302,6 +304,7 @@ NbrCtx make_ctx(const DeviceState &d, const PaperConsts &c, const uint16_t *sid)
   nc.scenes = d.scenes;
   nc.sid = sid;
   nc.err = d.err;
+  nc.cnt_max = d.nbr_max;
   nc.n = c.n;
   nc.maxn = c.maxn;
   nc.dt = c.dt;

@@ -24,9 +24,18 @@ struct NbrCtx {
   const SceneDesc *__restrict__ scenes;
   const uint16_t *__restrict__ sid;
   uint32_t *err;
+  uint32_t *cnt_max;  // largest neighbour count of the step (may be null)
   uint32_t n, maxn;
   float dt, h2;
 };
+
+// Folds the neighbour counts of the calling warp's active threads into the
+// step's largest count: one atomic per warp.
+__device__ __forceinline__ void record_count(uint32_t *cnt_max, uint32_t cnt) {
+  const unsigned m = __activemask();
+  const uint32_t mx = __reduce_max_sync(m, cnt);
+  if (cnt_max && (threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicMax(cnt_max, mx);
+}
 
 __device__ __forceinline__ const SceneDesc &scene_of(const SceneDesc *scenes,
                                                      const uint16_t *sid,
@@ -141,6 +150,28 @@ __device__ __forceinline__ bool is_pair(float r2, float h2) {
   return r2 >= 1.17549435e-38f && r2 < h2;
 }
 
+// All arithmetic on pair and particle values below is written with
+// explicitly rounded operations (__fadd_rn, __fmul_rn, __fmaf_rn, ...): the
+// compiler may not contract or reassociate them, so every kernel that
+// evaluates a pair -- fused or not, any launch shape, staged or through L1 --
+// rounds it the same way and gets the same bits.  (Left to itself, nvcc
+// contracts a*b + c*d into an FMA on either product, and its choice can
+// differ from one kernel to another.)
+struct Sep {
+  float x, y, z, r2;  // p_k - p_j and its squared length
+};
+__device__ __forceinline__ Sep separation(const float4 &a, const float4 &b) {
+  Sep r;
+  r.x = __fsub_rn(a.x, b.x);
+  r.y = __fsub_rn(a.y, b.y);
+  r.z = __fsub_rn(a.z, b.z);
+  r.r2 = __fmaf_rn(r.z, r.z, __fmaf_rn(r.y, r.y, __fmul_rn(r.x, r.x)));
+  return r;
+}
+__device__ __forceinline__ Sep separation(const float3 &a, const float3 &b) {
+  return separation(make_float4(a.x, a.y, a.z, 0.f), make_float4(b.x, b.y, b.z, 0.f));
+}
+
 // Visits the 9 rows around the cell with key `key` (order: dz, dy, slot);
 // f(q, j) gets the row index q = (dz+1)*3 + (dy+1) and the slot j != k.
 template <typename F>
@@ -176,10 +207,7 @@ __device__ __forceinline__ void visit_fallback(const NbrCtx &c, uint32_t k, F &&
   const SceneDesc &sc = scene_of(c.scenes, c.sid, k);
   const float3 pk = start_position(c, k);
   scan_rows(k, __ldg(&c.skeys[k]), sc, c.off, [&](int, uint32_t j) {
-    const float3 pj = start_position(c, j);
-    const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
-    const float r2 = rx * rx + ry * ry + rz * rz;
-    if (is_pair(r2, c.h2)) f(j);
+    if (is_pair(separation(pk, start_position(c, j)).r2, c.h2)) f(j);
   });
 }
 
@@ -200,8 +228,8 @@ __device__ __forceinline__ void visit_neighbours(const NbrCtx &c, uint32_t k, Lo
 __device__ __forceinline__ float ipow(float b, int e) {
   float r = 1.0f;
   while (e > 0) {
-    if (e & 1) r *= b;
-    b *= b;
+    if (e & 1) r = __fmul_rn(r, b);
+    b = __fmul_rn(b, b);
     e >>= 1;
   }
   return r;
@@ -211,13 +239,13 @@ __device__ __forceinline__ float ipow(float b, int e) {
 // kTwelve: the exponent 3n is 12 (n = 4, the paper's choice).
 template <bool kTwelve>
 __device__ __forceinline__ float scorr_term(float r2, const PaperConsts &c) {
-  const float ratio = (c.h2 - r2) * c.inv_scorr_den;
+  const float ratio = __fmul_rn(__fsub_rn(c.h2, r2), c.inv_scorr_den);
   if constexpr (kTwelve) {
-    const float r3 = ratio * ratio * ratio;
-    const float r6 = r3 * r3;
-    return -c.scorr_k * (r6 * r6);
+    const float r3 = __fmul_rn(__fmul_rn(ratio, ratio), ratio);
+    const float r6 = __fmul_rn(r3, r3);
+    return __fmul_rn(-c.scorr_k, __fmul_rn(r6, r6));
   } else {
-    return -c.scorr_k * ipow(ratio, c.scorr_n3);
+    return __fmul_rn(-c.scorr_k, ipow(ratio, c.scorr_n3));
   }
 }
 
@@ -227,30 +255,35 @@ __device__ __forceinline__ float scorr_term(float r2, const PaperConsts &c) {
 __device__ __forceinline__ float spiky_factor(float r2, const PaperConsts &c) {
   float rinv;
   asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rinv) : "f"(r2));
-  const float hr = c.h - r2 * rinv;
-  return -c.spiky * hr * hr * rinv;
+  const float hr = __fsub_rn(c.h, __fmul_rn(r2, rinv));
+  return __fmul_rn(__fmul_rn(__fmul_rn(-c.spiky, hr), hr), rinv);
+}
+
+// Poly6 kernel value W(r) = poly6 (h^2 - r^2)^3.
+__device__ __forceinline__ float poly6_value(float r2, const PaperConsts &c) {
+  const float t = __fsub_rn(c.h2, r2);
+  return __fmul_rn(__fmul_rn(__fmul_rn(c.poly6, t), t), t);
 }
 
 struct LambdaAcc {
   float rho, gx, gy, gz, s;
-  __device__ __forceinline__ void add(float rx, float ry, float rz, float r2,
-                                      const PaperConsts &c) {
-    const float t = c.h2 - r2;
-    rho += c.poly6 * t * t * t;
-    const float f = spiky_factor(r2, c);
-    gx += f * rx;
-    gy += f * ry;
-    gz += f * rz;
-    s += f * f * r2;
+  __device__ __forceinline__ void add(const Sep &r, const PaperConsts &c) {
+    rho = __fadd_rn(rho, poly6_value(r.r2, c));
+    const float f = spiky_factor(r.r2, c);
+    gx = __fmaf_rn(f, r.x, gx);
+    gy = __fmaf_rn(f, r.y, gy);
+    gz = __fmaf_rn(f, r.z, gz);
+    s = __fmaf_rn(__fmul_rn(f, f), r.r2, s);
   }
   __device__ __forceinline__ float lambda(const PaperConsts &c) const {
-    const float C = rho * c.inv_rho0 - 1.0f;
-    const float den = (gx * gx + gy * gy + gz * gz + s) * (c.inv_rho0 * c.inv_rho0);
-    return -C / (den + c.relax_eps);
+    const float C = __fmaf_rn(rho, c.inv_rho0, -1.0f);
+    const float g2 = __fmaf_rn(gz, gz, __fmaf_rn(gy, gy, __fmaf_rn(gx, gx, s)));
+    const float den = __fmul_rn(g2, __fmul_rn(c.inv_rho0, c.inv_rho0));
+    return __fdiv_rn(-C, __fadd_rn(den, c.relax_eps));
   }
 };
 
-// Calls member(j, rx, ry, rz, r2) for every slot j that forms a pair with k
+// Calls member(j, sep) for every slot j that forms a pair with k
 // (is_pair(r2 = |p_k - p_j|^2)) in the 27 cells around k's cell (key `key`),
 // in the order the lists store and the re-derived path visits: rows by
 // (dz, dy), each row's slots ascending.  The self pair and coincident
@@ -287,9 +320,8 @@ __device__ __forceinline__ void scan_members(const float4 &pk, uint32_t key, con
         for (int e = 0; e < 4; ++e) d[e] = __ldg(q + e);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-          const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
-          const float r2 = rx * rx + ry * ry + rz * rz;
-          if (is_pair(r2, c.h2)) member(j + e, rx, ry, rz, r2);
+          const Sep r = separation(pk, d[e]);
+          if (is_pair(r.r2, c.h2)) member(j + e, r);
         }
       }
       if (j < b) {
@@ -298,9 +330,8 @@ __device__ __forceinline__ void scan_members(const float4 &pk, uint32_t key, con
         for (int e = 0; e < 3; ++e) d[e] = __ldg(&P[min(j + e, b - 1u)]);
 #pragma unroll
         for (int e = 0; e < 3; ++e) {
-          const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
-          const float r2 = rx * rx + ry * ry + rz * rz;
-          if (j + e < b && is_pair(r2, c.h2)) member(j + e, rx, ry, rz, r2);
+          const Sep r = separation(pk, d[e]);
+          if (j + e < b && is_pair(r.r2, c.h2)) member(j + e, r);
         }
       }
     }
@@ -319,9 +350,8 @@ __device__ __forceinline__ void pad_list(uint32_t *__restrict__ out, size_t stri
 // Lambda pass: density, constraint gradient sums over the pairs of k.
 __device__ __forceinline__ void lambda_pair(LambdaAcc &acc, const float4 &pk, const float4 &pj,
                                             const PaperConsts &c) {
-  const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
-  const float r2 = rx * rx + ry * ry + rz * rz;
-  if (is_pair(r2, c.h2)) acc.add(rx, ry, rz, r2, c);
+  const Sep r = separation(pk, pj);
+  if (is_pair(r.r2, c.h2)) acc.add(r, c);
 }
 __device__ __forceinline__ void lambda_commit(uint32_t k, const float4 &pk, const LambdaAcc &acc,
                                               const PaperConsts &c, float4 *__restrict__ Q,
@@ -335,13 +365,13 @@ struct DeltaAcc {
   float sx, sy, sz;
   template <bool kTwelve>
   __device__ __forceinline__ void pair(const float4 &qk, const float4 &qj, const PaperConsts &c) {
-    const float rx = qk.x - qj.x, ry = qk.y - qj.y, rz = qk.z - qj.z;
-    const float r2 = rx * rx + ry * ry + rz * rz;
-    if (is_pair(r2, c.h2)) {
-      const float wgt = (qk.w + qj.w + scorr_term<kTwelve>(r2, c)) * spiky_factor(r2, c);
-      sx += wgt * rx;
-      sy += wgt * ry;
-      sz += wgt * rz;
+    const Sep r = separation(qk, qj);
+    if (is_pair(r.r2, c.h2)) {
+      const float wgt = __fmul_rn(__fadd_rn(__fadd_rn(qk.w, qj.w), scorr_term<kTwelve>(r.r2, c)),
+                                  spiky_factor(r.r2, c));
+      sx = __fmaf_rn(wgt, r.x, sx);
+      sy = __fmaf_rn(wgt, r.y, sy);
+      sz = __fmaf_rn(wgt, r.z, sz);
     }
   }
 };
@@ -354,22 +384,22 @@ __device__ __forceinline__ void delta_commit(uint32_t k, const DeltaAcc &a, cons
                                              float4 *__restrict__ U, int last) {
   const float4 x = load_own(&nc.X2[k]);
   const float4 d0 = load_own(&D[k]);
-  float3 d = make_float3(d0.x + a.sx * c.inv_rho0, d0.y + a.sy * c.inv_rho0,
-                         d0.z + a.sz * c.inv_rho0);
+  float3 d = make_float3(__fmaf_rn(a.sx, c.inv_rho0, d0.x), __fmaf_rn(a.sy, c.inv_rho0, d0.y),
+                         __fmaf_rn(a.sz, c.inv_rho0, d0.z));
   float3 p = add3(x, d);
   const SceneDesc &sc = scene_of(nc.scenes, nc.sid, k);
-  const float lo_x = sc.lo[0] + sc.wave;
-  if (p.x < lo_x) { d.x = lo_x - x.x; p.x = x.x + d.x; }
-  else if (p.x > sc.hi[0]) { d.x = sc.hi[0] - x.x; p.x = x.x + d.x; }
-  if (p.y < sc.lo[1]) { d.y = sc.lo[1] - x.y; p.y = x.y + d.y; }
-  else if (p.y > sc.hi[1]) { d.y = sc.hi[1] - x.y; p.y = x.y + d.y; }
-  if (p.z < sc.lo[2]) { d.z = sc.lo[2] - x.z; p.z = x.z + d.z; }
-  else if (p.z > sc.hi[2]) { d.z = sc.hi[2] - x.z; p.z = x.z + d.z; }
+  const float lo_x = __fadd_rn(sc.lo[0], sc.wave);
+  if (p.x < lo_x) { d.x = __fsub_rn(lo_x, x.x); p.x = __fadd_rn(x.x, d.x); }
+  else if (p.x > sc.hi[0]) { d.x = __fsub_rn(sc.hi[0], x.x); p.x = __fadd_rn(x.x, d.x); }
+  if (p.y < sc.lo[1]) { d.y = __fsub_rn(sc.lo[1], x.y); p.y = __fadd_rn(x.y, d.y); }
+  else if (p.y > sc.hi[1]) { d.y = __fsub_rn(sc.hi[1], x.y); p.y = __fadd_rn(x.y, d.y); }
+  if (p.z < sc.lo[2]) { d.z = __fsub_rn(sc.lo[2], x.z); p.z = __fadd_rn(x.z, d.z); }
+  else if (p.z > sc.hi[2]) { d.z = __fsub_rn(sc.hi[2], x.z); p.z = __fadd_rn(x.z, d.z); }
   D[k] = make_float4(d.x, d.y, d.z, 0.0f);
   P[k] = make_float4(p.x, p.y, p.z, 0.0f);
   if (last)
-    U[k] = make_float4(__fdiv_rn(d.x, c.dt), __fdiv_rn(d.y, c.dt),
-                       __fdiv_rn(d.z, c.dt), 1.0f / load_own(&R[k]));
+    U[k] = make_float4(__fdiv_rn(d.x, c.dt), __fdiv_rn(d.y, c.dt), __fdiv_rn(d.z, c.dt),
+                       __fdiv_rn(1.0f, load_own(&R[k])));
 }
 
 // A neighbour's (position, velocity) as the velocity passes read it.
@@ -377,29 +407,36 @@ struct PU {
   float4 p, u;
 };
 
+// a x b, component by component with one rounding per product and sum.
+__device__ __forceinline__ float cross_component(float a1, float b2, float a2, float b1) {
+  return __fmaf_rn(a1, b2, __fmul_rn(-a2, b1));  // a1 b2 - a2 b1
+}
+
 // Vorticity pass: omega_k = sum (1/rho_j) grad W x (v_j - v_k).
 struct VortAcc {
   float wx, wy, wz;
   __device__ __forceinline__ void pair(const float4 &pk, const float4 &uk, const PU &d,
                                        const PaperConsts &c) {
-    const float4 pj = d.p;
-    const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
-    const float r2 = rx * rx + ry * ry + rz * rz;
-    if (is_pair(r2, c.h2)) {
+    const Sep r = separation(pk, d.p);
+    if (is_pair(r.r2, c.h2)) {
       const float4 uj = d.u;
-      const float f = spiky_factor(r2, c) * uj.w;
-      const float gx = f * rx, gy = f * ry, gz = f * rz;
-      const float ux = uj.x - uk.x, uy = uj.y - uk.y, uz = uj.z - uk.z;
-      wx += gy * uz - gz * uy;
-      wy += gz * ux - gx * uz;
-      wz += gx * uy - gy * ux;
+      const float f = __fmul_rn(spiky_factor(r.r2, c), uj.w);
+      const float gx = __fmul_rn(f, r.x), gy = __fmul_rn(f, r.y), gz = __fmul_rn(f, r.z);
+      const float ux = __fsub_rn(uj.x, uk.x), uy = __fsub_rn(uj.y, uk.y),
+                  uz = __fsub_rn(uj.z, uk.z);
+      wx = __fadd_rn(wx, cross_component(gy, uz, gz, uy));
+      wy = __fadd_rn(wy, cross_component(gz, ux, gx, uz));
+      wz = __fadd_rn(wz, cross_component(gx, uy, gy, ux));
     }
   }
 };
+__device__ __forceinline__ float norm3(float x, float y, float z) {
+  return __fsqrt_rn(__fmaf_rn(z, z, __fmaf_rn(y, y, __fmul_rn(x, x))));
+}
 // Writes omega_k with |omega_k|, and (p_k, |omega_k|) for the XSPH pass.
 __device__ __forceinline__ void vort_commit(uint32_t k, const float4 &pk, const VortAcc &a,
                                             float4 *__restrict__ Wo, float4 *__restrict__ PW) {
-  const float wn = sqrtf(a.wx * a.wx + a.wy * a.wy + a.wz * a.wz);
+  const float wn = norm3(a.wx, a.wy, a.wz);
   Wo[k] = make_float4(a.wx, a.wy, a.wz, wn);
   PW[k] = make_float4(pk.x, pk.y, pk.z, wn);
 }
@@ -411,19 +448,17 @@ struct XsphAcc {
   __device__ __forceinline__ void pair(const float4 &pk, const float4 &uk, const float4 &wk,
                                        const PU &d, const PaperConsts &c) {
     const float4 pj = d.p;
-    const float rx = pk.x - pj.x, ry = pk.y - pj.y, rz = pk.z - pj.z;
-    const float r2 = rx * rx + ry * ry + rz * rz;
-    if (is_pair(r2, c.h2)) {
+    const Sep r = separation(pk, pj);
+    if (is_pair(r.r2, c.h2)) {
       const float4 uj = d.u;
-      const float e = spiky_factor(r2, c) * uj.w * (pj.w - wk.w);
-      ex += e * rx;
-      ey += e * ry;
-      ez += e * rz;
-      const float t = c.h2 - r2;
-      const float wp = c.poly6 * t * t * t * uj.w;
-      xx += wp * (uj.x - uk.x);
-      xy += wp * (uj.y - uk.y);
-      xz += wp * (uj.z - uk.z);
+      const float e = __fmul_rn(__fmul_rn(spiky_factor(r.r2, c), uj.w), __fsub_rn(pj.w, wk.w));
+      ex = __fmaf_rn(e, r.x, ex);
+      ey = __fmaf_rn(e, r.y, ey);
+      ez = __fmaf_rn(e, r.z, ez);
+      const float wp = __fmul_rn(poly6_value(r.r2, c), uj.w);
+      xx = __fmaf_rn(wp, __fsub_rn(uj.x, uk.x), xx);
+      xy = __fmaf_rn(wp, __fsub_rn(uj.y, uk.y), xy);
+      xz = __fmaf_rn(wp, __fsub_rn(uj.z, uk.z), xz);
     }
   }
 };
@@ -434,21 +469,21 @@ __device__ __forceinline__ void xsph_commit(uint32_t k, const float4 &pk, const 
                                             const PaperConsts &c, const uint32_t *__restrict__ ID2,
                                             float4 *__restrict__ X, float4 *__restrict__ V,
                                             uint32_t *__restrict__ ID) {
-  const float el2 = a.ex * a.ex + a.ey * a.ey + a.ez * a.ez;
+  const float el2 = __fmaf_rn(a.ez, a.ez, __fmaf_rn(a.ey, a.ey, __fmul_rn(a.ex, a.ex)));
   float nx = 0.f, ny = 0.f, nz = 0.f;
   if (el2 > 0.0f) {
     const float inv = rsqrtf(el2);
-    nx = a.ex * inv;
-    ny = a.ey * inv;
-    nz = a.ez * inv;
+    nx = __fmul_rn(a.ex, inv);
+    ny = __fmul_rn(a.ey, inv);
+    nz = __fmul_rn(a.ez, inv);
   }
-  const float fx = c.vort_eps * (ny * wk.z - nz * wk.y);
-  const float fy = c.vort_eps * (nz * wk.x - nx * wk.z);
-  const float fz = c.vort_eps * (nx * wk.y - ny * wk.x);
-  const float vx = uk.x + c.dt * fx + c.xsph_c * a.xx;
-  const float vy = uk.y + c.dt * fy + c.xsph_c * a.xy;
-  const float vz = uk.z + c.dt * fz + c.xsph_c * a.xz;
-  X[k] = make_float4(pk.x, pk.y, pk.z, sqrtf(vx * vx + vy * vy + vz * vz));
+  const float fx = __fmul_rn(c.vort_eps, cross_component(ny, wk.z, nz, wk.y));
+  const float fy = __fmul_rn(c.vort_eps, cross_component(nz, wk.x, nx, wk.z));
+  const float fz = __fmul_rn(c.vort_eps, cross_component(nx, wk.y, ny, wk.x));
+  const float vx = __fmaf_rn(c.xsph_c, a.xx, __fmaf_rn(c.dt, fx, uk.x));
+  const float vy = __fmaf_rn(c.xsph_c, a.xy, __fmaf_rn(c.dt, fy, uk.y));
+  const float vz = __fmaf_rn(c.xsph_c, a.xz, __fmaf_rn(c.dt, fz, uk.z));
+  X[k] = make_float4(pk.x, pk.y, pk.z, norm3(vx, vy, vz));
   V[k] = make_float4(vx, vy, vz, load_own(&nc.V2[k]).w);
   ID[k] = load_own(&ID2[k]);
 }

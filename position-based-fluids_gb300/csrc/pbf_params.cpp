@@ -225,6 +225,7 @@ void pbf_params_default(pbf_params *p) {
   p->gravity_y = -9.81f;
   p->wall_margin = -1.0f; /* resolved to h/4 */
   p->max_neighbours = 128;
+  p->grow_lists = 1;
 }
 
 }  // extern "C"

@@ -136,6 +136,7 @@ int pbf_read_config(const char *path, pbf_params *out) {
     else if (key == "gravity_y") ok = bool(ss >> out->gravity_y);
     else if (key == "wall_margin") ok = bool(ss >> out->wall_margin);
     else if (key == "max_neighbours") ok = bool(ss >> out->max_neighbours);
+    else if (key == "grow_lists") ok = bool(ss >> out->grow_lists);
     else {
       std::cerr << "Unknown parameter " << key << std::endl
                 << "Leaving it out." << std::endl;
@@ -286,14 +287,16 @@ int pbf_write_config(const char *path, const pbf_params *p) {
                "vort_eps              %.9g\n"
                "gravity_y             %.9g\n"
                "wall_margin           %.9g\n"
-               "max_neighbours        %u\n",
+               "max_neighbours        %u\n"
+               "grow_lists            %u\n",
                p->time_end, p->time_step_length, p->x_min, p->x_max,
                p->y_min, p->y_max, p->z_min, p->z_max, p->x_n, p->y_n, p->z_n,
                p->rest_density, p->part_out_freq,
                p->part_out_name_base[0] ? p->part_out_name_base : "part",
                p->vtk_out_freq, p->vtk_out_name_base[0] ? p->vtk_out_name_base : "vtk", mode,
                p->solver_iterations, p->relax_eps, p->scorr_k, p->scorr_dq, p->scorr_n,
-               p->xsph_c, p->vort_eps, p->gravity_y, p->wall_margin, p->max_neighbours);
+               p->xsph_c, p->vort_eps, p->gravity_y, p->wall_margin, p->max_neighbours,
+               p->grow_lists);
   return std::fclose(f) == 0 ? PBF_OK : PBF_ERR_IO;
 }
 

@@ -62,6 +62,14 @@ struct pbf_sim {
   bool have_times = false;
   bool stepped = false;
   bool scene_dirty = false;
+  // adaptive neighbour-list capacity (paper): the largest count of each
+  // step lands in page-locked memory; before launching a step the host
+  // looks at the count of the step two back (the first step's right after
+  // it) and grows the lists when it came within 1/8 of the capacity
+  uint32_t *nbr_max_host = nullptr;
+  cudaEvent_t step_done[2] = {nullptr, nullptr};
+  uint64_t launched = 0;  // steps launched since init or the last growth
+  uint32_t list_grows = 0;
   // debug views
   int32_t *d_ranges = nullptr;
 };
@@ -83,6 +91,12 @@ int dalloc(pbf_sim *s, T **p, size_t count) {
 void free_all(pbf_sim *s) {
   if (s->graph) cudaGraphExecDestroy(s->graph);
   s->graph = nullptr;
+  for (cudaEvent_t &e : s->step_done) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
+  if (s->nbr_max_host) cudaFreeHost(s->nbr_max_host);
+  s->nbr_max_host = nullptr;
   for (cudaEvent_t e : s->events) cudaEventDestroy(e);
   s->events.clear();
   for (void *p : s->allocations) cudaFree(p);
@@ -155,12 +169,15 @@ int launch_step(pbf_sim *s) {
                           d.P, d.D, st));
     PBF_TRY_STATUS(mark(s, 0, "reorder", 1, &ev));
     const uint32_t iters = s->prm.solver_iterations;
+    PBF_TRY(cudaMemsetAsync(d.nbr_max, 0, sizeof(uint32_t), st));
     if (d.tune.staged) {
       PBF_TRY(tile_plan(d, s->pc, nullptr, st));
       PBF_TRY_STATUS(mark(s, 0, "tile_plan", 1, &ev));
       for (uint32_t it = 0; it < iters; ++it) {
         if (it == 0) {
           PBF_TRY(tile_nbr_build(d, s->pc, nullptr, st));
+          PBF_TRY(cudaMemcpyAsync(s->nbr_max_host, d.nbr_max, sizeof(uint32_t),
+                                  cudaMemcpyDeviceToHost, st));
           PBF_TRY_STATUS(mark(s, 1, "nbr_build", 1, &ev));
         }
         PBF_TRY(tile_lambda(d, s->pc, nullptr, st));
@@ -176,10 +193,14 @@ int launch_step(pbf_sim *s) {
       for (uint32_t it = 0; it < iters; ++it) {
         if (it == 0 && d.tune.fuse_first) {
           PBF_TRY(paper_nbr_lambda(d, s->pc, nullptr, st));
+          PBF_TRY(cudaMemcpyAsync(s->nbr_max_host, d.nbr_max, sizeof(uint32_t),
+                                  cudaMemcpyDeviceToHost, st));
           PBF_TRY_STATUS(mark(s, 1, "nbr_lambda", 1, &ev));
         } else {
           if (it == 0) {
             PBF_TRY(paper_nbr_build(d, s->pc, nullptr, st));
+            PBF_TRY(cudaMemcpyAsync(s->nbr_max_host, d.nbr_max, sizeof(uint32_t),
+                                    cudaMemcpyDeviceToHost, st));
             PBF_TRY_STATUS(mark(s, 1, "nbr_build", 1, &ev));
           }
           PBF_TRY(paper_lambda(d, s->pc, nullptr, st));
@@ -290,6 +311,46 @@ int collect_times(pbf_sim *s) {
 
 bool ready(const pbf_sim *s) { return s && s->inited; }
 
+// Largest list capacity (pbf_params.max_neighbours range).
+constexpr uint32_t kMaxListCapacity = 1024;
+
+// Before a paper-mode step: the largest neighbour count of a recent step
+// (the first step's right after it, later the step two back, which leaves
+// one step queued on the device while the host waits) against the list
+// capacity.  When it came within 1/8 of the capacity the lists grow to 1.5x
+// that count (multiple of 8, at most 1024) before the step is launched, so a
+// scene whose sets outgrow the lists re-derives them from the cells in at
+// most the steps already queued.
+int adapt_lists(pbf_sim *s) {
+  if (!s->paper || !s->prm.grow_lists || s->launched == 0) return PBF_OK;
+  const uint64_t wait_for = s->launched >= 2 ? s->launched - 2 : 0;
+  PBF_TRY(cudaEventSynchronize(s->step_done[wait_for & 1]));
+  const uint32_t mx = *reinterpret_cast<volatile uint32_t *>(s->nbr_max_host);
+  const uint32_t cap = s->pc.maxn;
+  if (cap >= kMaxListCapacity || mx <= cap - cap / 8) return PBF_OK;
+  const uint32_t grown = std::min(kMaxListCapacity, ((mx + mx / 2 + 7) / 8) * 8);
+  if (grown <= cap) return PBF_OK;
+  PBF_TRY(cudaStreamSynchronize(s->stream));
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  s->graph = nullptr;
+  DeviceState &d = s->d;
+  const size_t old_bytes = (size_t)paper_list_words(cap) * s->n * sizeof(uint4);
+  const size_t new_bytes = (size_t)paper_list_words(grown) * s->n * sizeof(uint4);
+  void *q = nullptr;
+  PBF_TRY(cudaMalloc(&q, std::max<size_t>(new_bytes, 16)));
+  for (void *&a : s->allocations)
+    if (a == d.nbr) {
+      cudaFree(a);
+      a = q;
+    }
+  d.nbr = static_cast<uint4 *>(q);
+  s->device_bytes += new_bytes - std::max<size_t>(old_bytes, 16);
+  s->pc.maxn = grown;
+  s->launched = 0;
+  ++s->list_grows;
+  return PBF_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -354,6 +415,7 @@ int pbf_init(pbf_sim *s) {
     A(&d.W, n);
     A(&d.R, n);
     A(&d.nbr_cnt, n);
+    A(&d.nbr_max, 1);
     A(&d.nbr, (size_t)paper_list_words(s->pc.maxn) * n);
     A(&d.tile_info, tile_count(s->n));
     A(&d.tile_seg, (size_t)tile_count(s->n) * kTileSegs);
@@ -366,8 +428,12 @@ int pbf_init(pbf_sim *s) {
     A(&d.SS, n);
   }
   if (rc == PBF_OK && s->paper) {
-    const cudaError_t te = tile_init();
-    if (te != cudaSuccess) rc = cuda_status(te, "tile_init");
+    cudaError_t te = tile_init();
+    if (te == cudaSuccess) te = cudaMallocHost(&s->nbr_max_host, sizeof(uint32_t));
+    for (cudaEvent_t &e : s->step_done)
+      if (te == cudaSuccess) te = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (te != cudaSuccess) rc = cuda_status(te, "pbf_init");
+    else *s->nbr_max_host = 0;
   }
   if (rc != PBF_OK) {
     free_all(s);
@@ -401,6 +467,7 @@ int pbf_step(pbf_sim *s, uint32_t nsteps) {
   if (!ready(s)) return PBF_ERR_STATE;
   for (uint32_t k = 0; k < nsteps; ++k) {
     if (s->scene_dirty) PBF_TRY_STATUS(upload_scene(s));
+    PBF_TRY_STATUS(adapt_lists(s));
     if (s->timing) {
       PBF_TRY_STATUS(launch_step(s));
       PBF_TRY_STATUS(collect_times(s));
@@ -410,8 +477,19 @@ int pbf_step(pbf_sim *s, uint32_t nsteps) {
     } else {
       PBF_TRY_STATUS(launch_step(s));
     }
+    if (s->paper) {
+      PBF_TRY(cudaEventRecord(s->step_done[s->launched & 1], s->stream));
+      ++s->launched;
+    }
     s->stepped = true;
   }
+  return PBF_OK;
+}
+
+int pbf_list_capacity(const pbf_sim *s, uint32_t *capacity, uint32_t *grows) {
+  if (!s || !capacity) return PBF_ERR_INVALID;
+  *capacity = s->pc.maxn;
+  if (grows) *grows = s->list_grows;
   return PBF_OK;
 }
 

@@ -368,12 +368,13 @@ __global__ void __launch_bounds__(kTile)
     uint32_t *__restrict__ out = reinterpret_cast<uint32_t *>(nbr4) + 4ull * k;
     const size_t stride = 4ull * c.n;
     uint32_t cnt = 0;
-    scan_members(pk, key, s, nc.off, P, c, [&](uint32_t j, float, float, float, float) {
+    scan_members(pk, key, s, nc.off, P, c, [&](uint32_t j, const Sep &) {
       if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j;
       ++cnt;
     });
     pad_list(out, stride, cnt, c.maxn, k);
     nbr_cnt[k] = cnt;
+    record_count(nc.cnt_max, cnt);
     return;
   }
   const float4 *__restrict__ stage = sm.stage(0);
@@ -408,23 +409,19 @@ __global__ void __launch_bounds__(kTile)
 #pragma unroll
         for (int e = 0; e < 4; ++e) d[e] = stage[(j + e) & (kStageCap - 1u)];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const float rx = pk.x - d[e].x, ry = pk.y - d[e].y, rz = pk.z - d[e].z;
-          const float r2 = rx * rx + ry * ry + rz * rz;
-          if (is_pair(r2, c.h2)) pack.push(j + e, out, stride, c.maxn);
-        }
+        for (int e = 0; e < 4; ++e)
+          if (is_pair(separation(pk, d[e]).r2, c.h2)) pack.push(j + e, out, stride, c.maxn);
       }
       for (; j < b; ++j) {
-        const float4 dj = stage[j & (kStageCap - 1u)];
-        const float rx = pk.x - dj.x, ry = pk.y - dj.y, rz = pk.z - dj.z;
-        const float r2 = rx * rx + ry * ry + rz * rz;
-        if (is_pair(r2, c.h2)) pack.push(j, out, stride, c.maxn);
+        if (is_pair(separation(pk, stage[j & (kStageCap - 1u)]).r2, c.h2))
+          pack.push(j, out, stride, c.maxn);
       }
     }
   }
   const uint2 own = seg[4];  // the particle's own row
   pack.finish(k - own.x + own.y, out, stride, c.maxn);
   nbr_cnt[k] = pack.cnt;
+  record_count(nc.cnt_max, pack.cnt);
 }
 
 __global__ void __launch_bounds__(kTile)
@@ -554,6 +551,7 @@ NbrCtx make_ctx(const DeviceState &d, const PaperConsts &c, const uint16_t *sid)
   nc.scenes = d.scenes;
   nc.sid = sid;
   nc.err = d.err;
+  nc.cnt_max = d.nbr_max;
   nc.n = c.n;
   nc.maxn = c.maxn;
   nc.dt = c.dt;

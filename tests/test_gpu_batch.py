@@ -87,6 +87,7 @@ def test_batch_neighbour_stats_match_the_plain_simulations(pbf):
         for s in scenes:
             p = s.params.copy()
             p.max_neighbours = cap
+            p.grow_lists = 0
             with pbf.Simulation(p, s.particles) as sim:
                 sim.init()
                 sim.step(5)

@@ -57,6 +57,7 @@ def test_single_scene_1m(pbf):
     again = run(pbf, sc.params, sc.particles, STEPS)
     capped = sc.params.copy()
     capped.max_neighbours = 16
+    capped.grow_lists = 0
     small_lists = run(pbf, capped, sc.particles, STEPS)
     with pbf.Batch(sc.params, 1, sc.n, sc.params.ncells) as bt:
         sid = bt.add_scene(sc.params, sc.particles)

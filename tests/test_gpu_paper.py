@@ -107,6 +107,7 @@ def test_list_overflow_path_matches_list_path(pbf):
     sc = pbf.scenes.dam_break((16, 16, 16), (0.8, 0.8, 1.6), seed=6)
     small = sc.params.copy()
     small.max_neighbours = 12  # most particles have ~26-40 neighbours
+    small.grow_lists = 0
     a = gpu_steps(pbf, sc, 10)
     b = gpu_steps(pbf, sc, 10, params=small)
     for x, y in zip(a, b):

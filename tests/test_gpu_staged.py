@@ -80,6 +80,7 @@ def test_staged_equals_l1_gathers(pbf, case):
         params, particles = sc.params.copy(), sc.particles
         if case == "capped_lists":
             params.max_neighbours = 16
+            params.grow_lists = 0
     elif case == "scattered":
         params, particles = scattered(pbf, 6000, (3.2, 3.2, 3.2), 42)
     else:
