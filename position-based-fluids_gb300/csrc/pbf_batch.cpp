@@ -48,8 +48,7 @@ size_t bytes_per_particle(uint32_t maxn) {
          + sizeof(float)                      // R
          + (size_t)paper_list_words(maxn) * 16  // lists
          + sizeof(uint16_t)                   // sid
-         + 2 * sizeof(float4)                 // io staging
-         + (4 + kTileSegs * 8 + kTileSlots - 1) / kTileSlots;  // tile plan
+         + 2 * sizeof(float4);                // io staging
 }
 
 }  // namespace
@@ -106,18 +105,21 @@ int find_scene(const pbf_batch *b, uint32_t id) {
 int apply_layout(pbf_batch *b) {
   DeviceState &d = b->d;
   b->table.resize(b->scenes.size());
-  uint32_t p = 0, c = 0;
+  uint32_t p = 0, c = 0, blocks = 0;
   for (size_t i = 0; i < b->scenes.size(); ++i) {
     SceneRec &s = b->scenes[i];
     s.desc.p_begin = p;
     s.desc.p_end = p + s.n;
     s.desc.cell_base = c;
+    s.desc.block_base = blocks;
     b->table[i] = s.desc;
     p += s.n;
     c += s.cells;
+    blocks += scene_blocks(s.desc);
   }
   b->n_total = p;
   b->cells_total = c;
+  d.blk_total = blocks;
   b->pc.n = p;
   b->plan = make_sort_plan(p, bits_for(std::max<uint32_t>(c, 1)));
   if (!b->scenes.empty()) {
@@ -145,14 +147,14 @@ int launch_batch_step(pbf_batch *b) {
   PBF_TRY(paper_reorder(d.perm, d.X, d.V, d.ID, n, pc, d.X2, d.V2, d.ID2, d.P, d.D, st));
   const uint32_t iters = b->solver.solver_iterations;
   if (d.tune.staged) {
-    PBF_TRY(tile_plan(d, pc, d.sid, st));
+    PBF_TRY(tile_plan(d, pc, d.sid, (uint32_t)b->scenes.size(), st));
     for (uint32_t it = 0; it < iters; ++it) {
-      if (it == 0) PBF_TRY(tile_nbr_build(d, pc, d.sid, st));
-      PBF_TRY(tile_lambda(d, pc, d.sid, st));
-      PBF_TRY(tile_delta(d, pc, d.sid, it + 1 == iters, st));
+      if (it == 0) PBF_TRY(tile_nbr_build(d, pc, d.sid, (uint32_t)b->scenes.size(), st));
+      PBF_TRY(tile_lambda(d, pc, d.sid, (uint32_t)b->scenes.size(), st));
+      PBF_TRY(tile_delta(d, pc, d.sid, (uint32_t)b->scenes.size(), it + 1 == iters, st));
     }
-    PBF_TRY(tile_vorticity(d, pc, d.sid, st));
-    PBF_TRY(tile_xsph_commit(d, pc, d.sid, st));
+    PBF_TRY(tile_vorticity(d, pc, d.sid, (uint32_t)b->scenes.size(), st));
+    PBF_TRY(tile_xsph_commit(d, pc, d.sid, (uint32_t)b->scenes.size(), st));
     return PBF_OK;
   }
   for (uint32_t it = 0; it < iters; ++it) {
@@ -220,6 +222,7 @@ size_t pbf_batch_device_bytes(const pbf_params *solver, uint32_t max_scenes,
   const SortPlan plan = make_sort_plan(max_particles, 32);
   return (size_t)max_particles * bytes_per_particle(pc.maxn) +
          ((size_t)max_cells + 1) * sizeof(uint32_t) +
+         (size_t)max_cells * sizeof(uint32_t) + 3 * sizeof(uint32_t) +  // cell-block list
          (size_t)offset_runs_capacity(max_cells) * sizeof(uint4) + sizeof(uint32_t) +
          plan.words * sizeof(uint32_t) +
          (size_t)max_scenes * sizeof(SceneDesc) + 64;
@@ -263,9 +266,10 @@ int pbf_batch_create(const pbf_params *solver, uint32_t max_scenes, uint32_t max
   A(&d.ID, M); A(&d.ID2, M); A(&d.keys, M); A(&d.skeys, M); A(&d.perm, M);
   A(&d.nbr_cnt, M); A(&d.R, M); A(&d.sid, M);
   A(&d.nbr, (size_t)paper_list_words(b->pc.maxn) * M);
-  A(&d.tile_info, tile_count(max_particles));
-  A(&d.tile_seg, (size_t)tile_count(max_particles) * kTileSegs);
-  A(&d.tile_stats, 2);
+  // every cell block holds at least one cell
+  d.blk_cap = max_cells;
+  A(&d.blk_list, d.blk_cap);
+  A(&d.blk_count, 3);
   A(&d.io_pos, M); A(&d.io_vel, M);
   A(&d.offsets, (size_t)max_cells + 1);
   A(&d.runs, offset_runs_capacity(max_cells));

@@ -32,7 +32,7 @@ struct SceneDesc {
   float wave;         // moving x-min wall offset
   uint32_t p_begin;   // first particle (sorted state)
   uint32_t p_end;     // one past the last particle
-  uint32_t pad_;
+  uint32_t block_base; // first cell-block index of this scene (staged passes)
 };
 
 // Solver constants of the paper equations (PBF_MODE_PAPER).
@@ -227,10 +227,11 @@ struct DeviceState {
   uint32_t *err = nullptr;             // device error flag word
   SceneDesc *scenes = nullptr;         // device scene table
   float4 *io_pos = nullptr, *io_vel = nullptr; // input-order staging
-  // staged tiles (paper): per tile of kTileSlots slots its plan
-  uint32_t *tile_info = nullptr;       // pieces and their first slots (0: not staged)
-  uint2 *tile_seg = nullptr;           // kTileSegs (first slot, length) per tile
-  uint32_t *tile_stats = nullptr;      // staged and unstaged tiles of the last plan
+  // staged cell blocks (paper): the step's work list of occupied blocks
+  uint32_t *blk_list = nullptr;        // block indices (capacity blk_cap)
+  uint32_t *blk_count = nullptr;       // [0] blocks in the list, [1] staged, [2] unstaged
+  uint32_t blk_cap = 0;                // capacity of blk_list
+  uint32_t blk_total = 0;              // blocks of the current layout (host)
   // batches only (null for a single scene)
   uint16_t *sid = nullptr;             // scene of each sorted slot
   // host-side launch shape of the gather passes, and the tuner's timer
@@ -244,29 +245,39 @@ cudaError_t scene_ids(const SceneDesc *scenes, uint32_t nscenes, uint32_t n, uin
 // dst[i] = i for i in [0, n).
 cudaError_t iota_range(uint32_t *dst, uint32_t n, cudaStream_t st);
 
-// ------------------------------------------------------------ staged tiles
-// Sorted slots per tile of the staged gather passes (= threads per CTA), and
-// segment-table entries per tile (9 per grid row, at most three rows).
-constexpr uint32_t kTileSlots = 128;
-constexpr uint32_t kTileSegs = 32;
-uint32_t tile_count(uint32_t n);
-// Sets the kernels' shared-memory limits (once per process); the launches
-// below call it too.
+// ------------------------------------------------------- staged cell blocks
+// The staged gather passes (pbf_tile.cu) work on blocks of kBlockCells^3
+// cells of each scene's grid.
+constexpr int kBlockCells = 4;
+#ifdef __CUDACC__
+#define PBF_HOST_DEVICE __host__ __device__
+#else
+#define PBF_HOST_DEVICE
+#endif
+PBF_HOST_DEVICE inline uint32_t blocks_along(int32_t cells) {
+  return (uint32_t)((cells + kBlockCells - 1) / kBlockCells);
+}
+inline uint32_t scene_blocks(const SceneDesc &s) {
+  return blocks_along(s.ncell[0]) * blocks_along(s.ncell[1]) * blocks_along(s.ncell[2]);
+}
+// Sets the kernels' shared-memory limits and persistent grid sizes (once per
+// process); the launches below call it too.
 cudaError_t tile_init();
-// The step's tile plan (after the cell offsets), then the staged passes:
-// the same outputs as the paper_* launches of the same names.
+// The step's list of occupied cell blocks (after the cell offsets), then the
+// staged passes: the same outputs as the paper_* launches of the same names.
+// `nscenes` scene descriptors, `blocks` = the layout's blocks in total.
 cudaError_t tile_plan(const DeviceState &d, const PaperConsts &c, const uint16_t *sid,
-                      cudaStream_t st);
+                      uint32_t nscenes, cudaStream_t st);
 cudaError_t tile_nbr_build(const DeviceState &d, const PaperConsts &c, const uint16_t *sid,
-                           cudaStream_t st);
+                           uint32_t nscenes, cudaStream_t st);
 cudaError_t tile_lambda(const DeviceState &d, const PaperConsts &c, const uint16_t *sid,
-                        cudaStream_t st);
-cudaError_t tile_delta(const DeviceState &d, const PaperConsts &c, const uint16_t *sid, bool last,
-                       cudaStream_t st);
+                        uint32_t nscenes, cudaStream_t st);
+cudaError_t tile_delta(const DeviceState &d, const PaperConsts &c, const uint16_t *sid,
+                       uint32_t nscenes, bool last, cudaStream_t st);
 cudaError_t tile_vorticity(const DeviceState &d, const PaperConsts &c, const uint16_t *sid,
-                           cudaStream_t st);
+                           uint32_t nscenes, cudaStream_t st);
 cudaError_t tile_xsph_commit(const DeviceState &d, const PaperConsts &c, const uint16_t *sid,
-                             cudaStream_t st);
+                             uint32_t nscenes, cudaStream_t st);
 
 // ------------------------------------------------------- paper-mode launches
 // 16-byte list words per particle for a list capacity of maxn neighbours.

@@ -171,23 +171,23 @@ int launch_step(pbf_sim *s) {
     const uint32_t iters = s->prm.solver_iterations;
     PBF_TRY(cudaMemsetAsync(d.nbr_max, 0, sizeof(uint32_t), st));
     if (d.tune.staged) {
-      PBF_TRY(tile_plan(d, s->pc, nullptr, st));
+      PBF_TRY(tile_plan(d, s->pc, nullptr, 1, st));
       PBF_TRY_STATUS(mark(s, 0, "tile_plan", 1, &ev));
       for (uint32_t it = 0; it < iters; ++it) {
         if (it == 0) {
-          PBF_TRY(tile_nbr_build(d, s->pc, nullptr, st));
+          PBF_TRY(tile_nbr_build(d, s->pc, nullptr, 1, st));
           PBF_TRY(cudaMemcpyAsync(s->nbr_max_host, d.nbr_max, sizeof(uint32_t),
                                   cudaMemcpyDeviceToHost, st));
           PBF_TRY_STATUS(mark(s, 1, "nbr_build", 1, &ev));
         }
-        PBF_TRY(tile_lambda(d, s->pc, nullptr, st));
+        PBF_TRY(tile_lambda(d, s->pc, nullptr, 1, st));
         PBF_TRY_STATUS(mark(s, 1, "lambda", 1, &ev));
-        PBF_TRY(tile_delta(d, s->pc, nullptr, it + 1 == iters, st));
+        PBF_TRY(tile_delta(d, s->pc, nullptr, 1, it + 1 == iters, st));
         PBF_TRY_STATUS(mark(s, 2, "delta", 1, &ev));
       }
-      PBF_TRY(tile_vorticity(d, s->pc, nullptr, st));
+      PBF_TRY(tile_vorticity(d, s->pc, nullptr, 1, st));
       PBF_TRY_STATUS(mark(s, 3, "vorticity", 1, &ev));
-      PBF_TRY(tile_xsph_commit(d, s->pc, nullptr, st));
+      PBF_TRY(tile_xsph_commit(d, s->pc, nullptr, 1, st));
       PBF_TRY_STATUS(mark(s, 3, "xsph_commit", 1, &ev));
     } else {
       for (uint32_t it = 0; it < iters; ++it) {
@@ -417,9 +417,9 @@ int pbf_init(pbf_sim *s) {
     A(&d.nbr_cnt, n);
     A(&d.nbr_max, 1);
     A(&d.nbr, (size_t)paper_list_words(s->pc.maxn) * n);
-    A(&d.tile_info, tile_count(s->n));
-    A(&d.tile_seg, (size_t)tile_count(s->n) * kTileSegs);
-    A(&d.tile_stats, 2);
+    d.blk_total = d.blk_cap = scene_blocks(s->scene);
+    A(&d.blk_list, d.blk_cap);
+    A(&d.blk_count, 3);
   } else {
     A(&d.PS, n);
     A(&d.PS2, n);
@@ -719,13 +719,13 @@ int pbf_neighbour_stats(pbf_sim *s, uint32_t *max_count, uint32_t *overflow) {
 int pbf_tile_stats(pbf_sim *s, uint32_t *staged, uint32_t *unstaged) {
   if (!ready(s) || !staged || !unstaged) return ready(s) ? PBF_ERR_INVALID : PBF_ERR_STATE;
   if (!s->paper || !s->stepped) return PBF_ERR_STATE;
-  uint32_t st[2] = {0u, 0u};
+  uint32_t st[3] = {0u, 0u, 0u};
   if (s->d.tune.staged) {
-    PBF_TRY(cudaMemcpyAsync(st, s->d.tile_stats, sizeof st, cudaMemcpyDeviceToHost, s->stream));
+    PBF_TRY(cudaMemcpyAsync(st, s->d.blk_count, sizeof st, cudaMemcpyDeviceToHost, s->stream));
     PBF_TRY(cudaStreamSynchronize(s->stream));
   }
-  *staged = st[0];
-  *unstaged = st[1];
+  *staged = st[1];
+  *unstaged = st[2];
   return PBF_OK;
 }
 
