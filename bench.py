@@ -441,10 +441,8 @@ def run_ours(args) -> int:
     if args.load_state:
         sim.load_state(args.load_state)
     tuning = None if args.no_tune else sim.autotune(3).as_dict()
-    if args.first_pass != "auto" or args.staged != "auto" or args.cell_build != "auto":
+    if args.first_pass != "auto" or args.staged != "auto":
         t = sim.tuning()
-        if args.cell_build != "auto":
-            t.cell_build = 1 if args.cell_build == "on" else 0
         if args.first_pass != "auto":
             t.fuse_first = 1 if args.first_pass == "fused" else 0
         if args.staged != "auto":
@@ -958,9 +956,6 @@ def main() -> int:
                     help="timed steps per scene of the one-by-one plain comparison")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-by-one plain comparison")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
-    ap.add_argument("--cell-build", choices=["auto", "on", "off"], default="auto",
-                    help="single and large scenes: list build with one warp per occupied cell, "
-                         "one thread per particle, or the tuner's (or default) choice")
     ap.add_argument("--staged", choices=["auto", "on", "off"], default="auto",
                     help="single and large scenes: gather passes on staged shared-memory tiles, "
                          "through L1, or the tuner's (or default) choice")

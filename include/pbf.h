@@ -229,17 +229,15 @@ int pbf_launches_per_step(const pbf_sim *sim, uint32_t *launches);
  * iteration.  staged = 1 runs every gather pass on staged tiles instead: a
  * CTA per 128 sorted slots copies its neighbourhood into shared memory with
  * bulk asynchronous copies and the passes read neighbours from there
- * (threads, batch and fuse_first then do not apply).  cell_build = 1 builds
- * the lists (not fused) with one warp per occupied cell, its lanes sharing
- * the cell's candidates.  No shape changes a result bit.  trial_ms is the
- * tuner's best time per launch of each pass (0 when untuned). */
+ * (threads, batch and fuse_first then do not apply).  No shape changes a
+ * result bit.  trial_ms is the tuner's best time per launch of each pass (0
+ * when untuned). */
 typedef struct pbf_tuning {
   uint32_t threads[6];
   uint32_t batch[6];
   uint32_t fuse_first;
   float trial_ms[6];
   uint32_t staged;
-  uint32_t cell_build;
 } pbf_tuning;
 /* Times every shape over `trial_steps` steps (1..32) of this simulation
  * from its current state, keeps the fastest per pass and restores the state

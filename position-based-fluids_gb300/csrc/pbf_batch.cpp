@@ -44,7 +44,7 @@ struct SceneRec {
 
 size_t bytes_per_particle(uint32_t maxn) {
   return 9 * sizeof(float4)                   // X V X2 V2 P Q D U W
-         + 7 * sizeof(uint32_t)               // ID ID2 keys skeys perm nbr_cnt cell_starts
+         + 6 * sizeof(uint32_t)               // ID ID2 keys skeys perm nbr_cnt
          + sizeof(float)                      // R
          + (size_t)paper_list_words(maxn) * 16  // lists
          + sizeof(uint16_t)                   // sid
@@ -161,9 +161,7 @@ int launch_batch_step(pbf_batch *b) {
     if (it == 0 && d.tune.fuse_first) {
       PBF_TRY(paper_nbr_lambda(d, pc, d.sid, st));
     } else {
-      if (it == 0)
-        PBF_TRY(d.tune.cell_build ? paper_nbr_build_cells(d, pc, d.sid, st)
-                                  : paper_nbr_build(d, pc, d.sid, st));
+      if (it == 0) PBF_TRY(paper_nbr_build(d, pc, d.sid, st));
       PBF_TRY(paper_lambda(d, pc, d.sid, st));
     }
     PBF_TRY(paper_delta(d, pc, d.sid, it + 1 == iters, st));
@@ -266,7 +264,7 @@ int pbf_batch_create(const pbf_params *solver, uint32_t max_scenes, uint32_t max
   A(&d.X, M); A(&d.V, M); A(&d.X2, M); A(&d.V2, M); A(&d.P, M); A(&d.Q, M);
   A(&d.D, M); A(&d.U, M); A(&d.W, M);
   A(&d.ID, M); A(&d.ID2, M); A(&d.keys, M); A(&d.skeys, M); A(&d.perm, M);
-  A(&d.nbr_cnt, M); A(&d.R, M); A(&d.sid, M); A(&d.cell_starts, M); A(&d.cell_count, 1);
+  A(&d.nbr_cnt, M); A(&d.R, M); A(&d.sid, M);
   A(&d.nbr, (size_t)paper_list_words(b->pc.maxn) * M);
   // every cell block holds at least one cell
   d.blk_cap = max_cells;

@@ -147,8 +147,6 @@ struct GatherTuning {
   // 1: the gather passes stage each tile's neighbourhood in shared memory
   // (pbf_tile.cu; one 128-thread shape, fuse_first does not apply)
   uint8_t staged = 0;
-  // 1: the L1 list build runs one warp per occupied cell (the same lists)
-  uint8_t cell_build = 0;
 };
 constexpr int kBlockCodes = 3;  // 64, 128, 256
 constexpr int kBatchCodes = 2;  // 4, 8
@@ -225,8 +223,6 @@ struct DeviceState {
   uint4 *nbr = nullptr;                // neighbour lists, 4 slots or 8 staged indices per word (paper)
   uint32_t *nbr_cnt = nullptr;         // neighbour counts (paper)
   uint32_t *nbr_max = nullptr;         // largest neighbour count of the step (paper)
-  uint32_t *cell_starts = nullptr;     // first slot of each occupied cell (paper, n)
-  uint32_t *cell_count = nullptr;      // occupied cells in cell_starts
   uint32_t *sort_scratch = nullptr;
   uint32_t *err = nullptr;             // device error flag word
   SceneDesc *scenes = nullptr;         // device scene table
@@ -298,17 +294,13 @@ cudaError_t paper_reorder(const uint32_t *perm, const float4 *X,
 // Neighbour lists of the step (from the predicted positions P).
 cudaError_t paper_nbr_build(const DeviceState &d, const PaperConsts &c,
                             const uint16_t *sid, cudaStream_t st);
-// The same lists, one warp per occupied cell (two launches and a memset).
-cudaError_t paper_nbr_build_cells(const DeviceState &d, const PaperConsts &c,
-                                  const uint16_t *sid, cudaStream_t st);
 // The same lists and, in the same kernel, the first lambda pass.
 cudaError_t paper_nbr_lambda(const DeviceState &d, const PaperConsts &c,
                              const uint16_t *sid, cudaStream_t st);
 // Launches of the first solver iteration's list build and lambda pass under
 // the current tuning (1 fused or 2).
 inline uint32_t paper_first_launches(const DeviceState &d) {
-  return d.tune.staged ? 3u /*plan, build, lambda*/
-                       : (d.tune.fuse_first ? 1u : (d.tune.cell_build ? 3u : 2u));
+  return d.tune.staged ? 3u /*plan, build, lambda*/ : (d.tune.fuse_first ? 1u : 2u);
 }
 cudaError_t paper_lambda(const DeviceState &d, const PaperConsts &c,
                          const uint16_t *sid, cudaStream_t st);

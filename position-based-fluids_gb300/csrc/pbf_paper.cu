@@ -166,164 +166,6 @@ __global__ void __launch_bounds__(kBlock)
   R[k] = acc.rho;
 }
 
-// ------------------------------------------------- list build, warp per cell
-// The particles of one cell share their 27-cell candidate sequence (9 rows
-// by (dz, dy), each row's slots ascending).  One warp takes one occupied cell
-// of m particles: with m <= 32 its lanes form m x (32 / m) (particle,
-// chunk) pairs, chunk ch testing the ch-th contiguous part of the sequence
-// for its particle; the lanes of one chunk read the same candidate at the
-// same time (one broadcast load), and every lane runs the same number of
-// tests.  Each lane keeps its chunk's members as a bitmask (chunks of at most
-// kChunkWords x 32 candidates), the warp adds up the chunk counts of each
-// particle, and every lane writes its members after those of the chunks
-// before it: the same members in the same order as k_nbr_build writes.
-// Cells of more than 32 particles, or with chunks too long for the mask,
-// take k_nbr_build's per-particle scan.
-constexpr uint32_t kChunkWords = 8;
-constexpr uint32_t kCellWarps = 8;  // warps per CTA
-
-// First slot of every occupied cell (a slot whose key differs from the
-// previous one), appended with one atomic per warp (*count starts at zero).
-__global__ void __launch_bounds__(256)
-    k_cell_starts(const uint32_t *__restrict__ skeys, uint32_t n, uint32_t *__restrict__ starts,
-                  uint32_t *__restrict__ count) {
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool start = s < n && (s == 0 || __ldg(&skeys[s]) != __ldg(&skeys[s - 1]));
-  const unsigned ball = __ballot_sync(0xffffffffu, start);
-  if (!ball) return;
-  const unsigned lane = threadIdx.x & 31u;
-  uint32_t base = 0;
-  if (lane == 0) base = atomicAdd(count, (uint32_t)__popc(ball));
-  base = __shfl_sync(0xffffffffu, base, 0);
-  if (start) starts[base + (uint32_t)__popc(ball & ((1u << lane) - 1u))] = s;
-}
-
-__global__ void __launch_bounds__(32 * kCellWarps)
-    k_nbr_build_cells(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
-                      const uint32_t *__restrict__ starts, const uint32_t *__restrict__ count,
-                      uint4 *__restrict__ nbr4, uint32_t *__restrict__ nbr_cnt) {
-  __shared__ uint2 s_rows[kCellWarps][10];  // per row q: (first slot, prefix); [9].y = total
-  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
-  uint2 *rows = s_rows[wib];
-  const uint32_t cells = __ldg(count);
-  const size_t stride = 4ull * c.n;  // 32-bit words from one list group to the next
-  for (uint32_t w = blockIdx.x * kCellWarps + wib; w < cells; w += gridDim.x * kCellWarps) {
-    const uint32_t s0 = __ldg(&starts[w]);
-    const uint32_t key = __ldg(&nc.skeys[s0]);
-    const uint32_t m = __ldg(&nc.off[key + 1]) - s0;
-    const SceneDesc &sc = scene_of(nc.scenes, nc.sid, s0);
-    const int nx = sc.ncell[0], ny = sc.ncell[1], nz = sc.ncell[2];
-    const uint32_t local = key - sc.cell_base;
-    const int cx = (int)(local % (uint32_t)nx);
-    const uint32_t tr = local / (uint32_t)nx;
-    const int cy = (int)(tr % (uint32_t)ny), cz = (int)(tr / (uint32_t)ny);
-    const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < nx ? cx + 1 : nx - 1;
-    uint32_t a = 0, len = 0;
-    if (lane < 9u) {
-      const int z = cz + (int)(lane / 3u) - 1, y = cy + (int)(lane % 3u) - 1;
-      if (z >= 0 && z < nz && y >= 0 && y < ny) {
-        const uint32_t row = sc.cell_base + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
-        a = __ldg(&nc.off[row + x0]);
-        len = __ldg(&nc.off[row + x1 + 1]) - a;
-      }
-    }
-    uint32_t incl = len;
-#pragma unroll
-    for (int o = 1; o < 16; o <<= 1) {
-      const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= (uint32_t)o) incl += v;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 8);
-    if (lane < 9u) rows[lane] = make_uint2(a, incl - len);
-    if (lane == 9u) rows[9] = make_uint2(0u, total);
-    __syncwarp();
-    const uint32_t chunks = m <= 32u ? 32u / m : 1u;
-    const bool cooperative = m <= 32u && (total + chunks - 1u) / chunks <= 32u * kChunkWords;
-    if (!cooperative) {
-      for (uint32_t i = lane; i < m; i += 32u) {
-        const uint32_t k = s0 + i;
-        const float4 pk = __ldg(&P[k]);
-        uint32_t *__restrict__ out = reinterpret_cast<uint32_t *>(nbr4) + 4ull * k;
-        uint32_t cnt = 0;
-        scan_members(pk, key, sc, nc.off, P, c, [&](uint32_t j, const Sep &) {
-          if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j;
-          ++cnt;
-        });
-        pad_list(out, stride, cnt, c.maxn, k);
-        nbr_cnt[k] = cnt;
-        record_count(nc.cnt_max, cnt);
-      }
-      __syncwarp();
-      continue;
-    }
-    const uint32_t i = lane % m, ch = lane / m;
-    const bool active = ch < chunks;
-    const uint32_t lo = active ? (uint32_t)((uint64_t)ch * total / chunks) : 0u;
-    const uint32_t hi = active ? (uint32_t)((uint64_t)(ch + 1u) * total / chunks) : 0u;
-    const float4 pi = __ldg(&P[s0 + i]);
-    // the row holding position lo
-    uint32_t q0 = 0;
-    while (q0 < 8u && rows[q0 + 1u].y <= lo) ++q0;
-    uint32_t mask[kChunkWords];
-    {
-      uint32_t q = q0, base = rows[q].x - rows[q].y, t1 = rows[q + 1u].y, p = lo;
-#pragma unroll
-      for (uint32_t wd = 0; wd < kChunkWords; ++wd) {
-        const uint32_t pe = min(hi, lo + 32u * (wd + 1u));
-        uint32_t bits = 0u;
-        while (p < pe) {
-          while (p >= t1) {
-            ++q;
-            base = rows[q].x - rows[q].y;
-            t1 = rows[q + 1u].y;
-          }
-          const uint32_t e = min(pe, t1);
-          for (; p < e; ++p)
-            if (is_pair(separation(pi, __ldg(&P[base + p])).r2, c.h2))
-              bits |= 1u << (p - lo - 32u * wd);
-        }
-        mask[wd] = bits;
-      }
-    }
-    uint32_t mine = 0;
-#pragma unroll
-    for (uint32_t wd = 0; wd < kChunkWords; ++wd) mine += (uint32_t)__popc(mask[wd]);
-    uint32_t before = 0, cnt = 0;
-    for (uint32_t c2 = 0; c2 < chunks; ++c2) {
-      const uint32_t v = __shfl_sync(0xffffffffu, mine, c2 * m + i);
-      before += c2 < ch ? v : 0u;
-      cnt += v;
-    }
-    if (active) {
-      const uint32_t k = s0 + i;
-      uint32_t *__restrict__ out = reinterpret_cast<uint32_t *>(nbr4) + 4ull * k;
-      uint32_t e = before;
-      uint32_t q = q0, base = rows[q].x - rows[q].y, t1 = rows[q + 1u].y;
-#pragma unroll
-      for (uint32_t wd = 0; wd < kChunkWords; ++wd) {
-        uint32_t bits = mask[wd];
-        while (bits) {
-          const uint32_t p = lo + 32u * wd + (uint32_t)(__ffs(bits) - 1);
-          bits &= bits - 1u;
-          while (p >= t1) {
-            ++q;
-            base = rows[q].x - rows[q].y;
-            t1 = rows[q + 1u].y;
-          }
-          if (e < c.maxn) out[(size_t)(e >> 2) * stride + (e & 3u)] = base + p;
-          ++e;
-        }
-      }
-      if (ch == chunks - 1u) {
-        pad_list(out, stride, cnt, c.maxn, k);
-        nbr_cnt[k] = cnt;
-      }
-    }
-    record_count(nc.cnt_max, cnt);
-    __syncwarp();
-  }
-}
-
 template <int kBlock, int kBatch>
 __global__ void __launch_bounds__(kBlock)
     k_lambda(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
@@ -524,20 +366,6 @@ cudaError_t paper_reorder(const uint32_t *perm, const float4 *X,
 cudaError_t paper_nbr_build(const DeviceState &d, const PaperConsts &c,
                             const uint16_t *sid, cudaStream_t st) {
   PBF_BUILD_LAUNCH(k_nbr_build, kKindNbr, d.P, make_ctx(d, c, sid), c, d.nbr, d.nbr_cnt);
-  return cudaGetLastError();
-}
-
-cudaError_t paper_nbr_build_cells(const DeviceState &d, const PaperConsts &c,
-                                  const uint16_t *sid, cudaStream_t st) {
-  if (c.n == 0) return cudaSuccess;
-  const int slot_ = d.timer ? d.timer->begin(kKindNbr, st) : -1;
-  cudaError_t e = cudaMemsetAsync(d.cell_count, 0, sizeof(uint32_t), st);
-  if (e != cudaSuccess) return e;
-  k_cell_starts<<<blocks_for(c.n, 256), 256, 0, st>>>(d.skeys, c.n, d.cell_starts, d.cell_count);
-  k_nbr_build_cells<<<kStrideCtas, 32 * kCellWarps, 0, st>>>(d.P, make_ctx(d, c, sid), c,
-                                                              d.cell_starts, d.cell_count, d.nbr,
-                                                              d.nbr_cnt);
-  if (d.timer) d.timer->end(slot_, st);
   return cudaGetLastError();
 }
 

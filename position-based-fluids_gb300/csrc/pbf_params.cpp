@@ -240,7 +240,6 @@ void to_pbf_tuning(const GatherTuning &g, const double trial_ms[kGatherKinds], p
   }
   out->fuse_first = g.fuse_first;
   out->staged = g.staged;
-  out->cell_build = g.cell_build;
 }
 
 int to_gather_tuning(const pbf_tuning &t, GatherTuning *out) {
@@ -268,11 +267,6 @@ int to_gather_tuning(const pbf_tuning &t, GatherTuning *out) {
     return PBF_ERR_INVALID;
   }
   g.staged = (uint8_t)t.staged;
-  if (t.cell_build > 1) {
-    set_error_message("tuning: cell_build must be 0 or 1");
-    return PBF_ERR_INVALID;
-  }
-  g.cell_build = (uint8_t)t.cell_build;
   *out = g;
   return PBF_OK;
 }

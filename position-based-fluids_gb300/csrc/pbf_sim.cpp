@@ -198,8 +198,7 @@ int launch_step(pbf_sim *s) {
           PBF_TRY_STATUS(mark(s, 1, "nbr_lambda", 1, &ev));
         } else {
           if (it == 0) {
-            PBF_TRY(d.tune.cell_build ? paper_nbr_build_cells(d, s->pc, nullptr, st)
-                                      : paper_nbr_build(d, s->pc, nullptr, st));
+            PBF_TRY(paper_nbr_build(d, s->pc, nullptr, st));
             PBF_TRY(cudaMemcpyAsync(s->nbr_max_host, d.nbr_max, sizeof(uint32_t),
                                     cudaMemcpyDeviceToHost, st));
             PBF_TRY_STATUS(mark(s, 1, "nbr_build", 1, &ev));
@@ -417,8 +416,6 @@ int pbf_init(pbf_sim *s) {
     A(&d.R, n);
     A(&d.nbr_cnt, n);
     A(&d.nbr_max, 1);
-    A(&d.cell_starts, n);
-    A(&d.cell_count, 1);
     A(&d.nbr, (size_t)paper_list_words(s->pc.maxn) * n);
     d.blk_total = d.blk_cap = scene_blocks(s->scene);
     A(&d.blk_list, d.blk_cap);

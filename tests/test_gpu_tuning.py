@@ -102,49 +102,3 @@ def test_batch_autotune_keeps_results(pbf):
     for a, c in zip(*out):
         for x, y in zip(a, c):
             assert np.array_equal(bits(x), bits(y))
-
-
-def test_cell_build_gives_the_same_bits(pbf):
-    """The list build with one warp per occupied cell (tuning cell_build)
-    writes the same lists as the per-particle build: same bits after 8 steps
-    on a dam break, with lists capped at 16 entries (overflowing sets), on a
-    sparse scene (one particle per cell: 32 chunks per particle), on a dense
-    block (64 particles per cell: the per-particle scan inside the warp) and
-    in a batch."""
-    sc = pbf.scenes.dam_break((16, 14, 12), (0.8, 1.6, 0.8), seed=31)
-    capped = sc.params.copy()
-    capped.max_neighbours = 16
-    capped.grow_lists = 0
-    rng = np.random.default_rng(5)
-    sparse = np.zeros(3000, pbf.PARTICLE_DTYPE)
-    sparse["x"] = rng.uniform(0.05, 3.15, size=(3000, 3)).astype(np.float32)
-    sparse["m"] = pbf.scenes.MASS
-    sparse_p = pbf.scenes.base_params((3.2, 3.2, 3.2), (32, 32, 32))
-    dense = pbf.generate_block((0.5, 0.5, 0.5), 16, 16, 16, 0.025, 0.0002, pbf.scenes.MASS / 64, 7)
-    dense_p = pbf.scenes.base_params((1.6, 1.6, 1.6), (16, 16, 16))
-    dense_p.rest_density = 1.0 / 0.025 ** 3
-    dense_p.max_neighbours = 512
-    for name, prm, ps in (("dam_break", sc.params, sc.particles), ("capped", capped, sc.particles),
-                          ("sparse", sparse_p, sparse), ("dense", dense_p, dense)):
-        scene = pbf.scenes.Scene(name, prm, ps, 8)
-        ref, launches = run(pbf, scene, 8)
-        t = shape(pbf, 128, 4, 0)
-        t.cell_build = 1
-        got, n = run(pbf, scene, 8, t)
-        for g, r in zip(got, ref):
-            assert np.array_equal(bits(g), bits(r)), name
-        assert n == launches + 1  # cell list and build instead of one build
-    scenes = pbf.scenes.mixed_batch(count=5, n_min=1000, n_max=20000, seed=3)
-    cap = (len(scenes), sum(s.n for s in scenes), sum(s.params.ncells for s in scenes))
-    out = []
-    for cell in (0, 1):
-        with pbf.Batch(scenes[0].params, *cap) as b:
-            ids = [b.add_scene(s.params, s.particles) for s in scenes]
-            t = b.tuning()
-            t.cell_build = cell
-            b.set_tuning(t)
-            b.step(6)
-            out.append([b.dump_scene(i) for i in ids])
-    for a, c in zip(*out):
-        for x, y in zip(a, c):
-            assert np.array_equal(bits(x), bits(y))
