@@ -413,11 +413,15 @@ def fp64_step_error(pbf, sim, params) -> dict:
     gpos, gvel = sim.dumpData()
     t0 = time.perf_counter()
     opos, ovel, *_ = oracle.paper_steps_f64(ge.paper_params_for_oracle(params), pos, vel, 1)
-    dx = np.abs(gpos[:, :3].astype(np.float64) - opos[:, :3]).max()
+    ex = np.abs(gpos[:, :3].astype(np.float64) - opos[:, :3]).max(axis=1) / params.h
     dv = np.abs(gvel[:, :3].astype(np.float64) - ovel[:, :3]).max()
-    return {"position_max_h": float(dx / params.h), "velocity_max": float(dv),
-            "bound_position_h": 1e-5, "within_bound": bool(dx <= 1e-5 * params.h),
-            "oracle_s": time.perf_counter() - t0,
+    # particles stacked on one point (clamped into a corner of the box) do
+    # not interact (r = 0) and can carry speeds where one step is chaotic
+    stacked = int(pos.shape[0] - np.unique(pos[:, :3], axis=0).shape[0])
+    return {"position_max_h": float(ex.max()), "position_p999_h": float(np.percentile(ex, 99.9)),
+            "particles_over_bound": int((ex > 1e-5).sum()), "velocity_max": float(dv),
+            "bound_position_h": 1e-5, "within_bound": bool(ex.max() <= 1e-5),
+            "stacked_particles": stacked, "oracle_s": time.perf_counter() - t0,
             "method": "one step from the state after the timed steps, GPU (binary32) against "
                       "the FP64 oracle restatement of the same equations from the same state"}
 

@@ -43,7 +43,7 @@ struct SceneRec {
 };
 
 size_t bytes_per_particle(uint32_t maxn) {
-  return 9 * sizeof(float4)                   // X V X2 V2 P Q D U W
+  return 10 * sizeof(float4)                  // X V X2 V2 P Q D U W S
          + 6 * sizeof(uint32_t)               // ID ID2 keys skeys perm nbr_cnt
          + sizeof(float)                      // R
          + (size_t)paper_list_words(maxn) * 16  // lists
@@ -262,7 +262,7 @@ int pbf_batch_create(const pbf_params *solver, uint32_t max_scenes, uint32_t max
     if (rc == PBF_OK) rc = balloc(b.get(), p, count);
   };
   A(&d.X, M); A(&d.V, M); A(&d.X2, M); A(&d.V2, M); A(&d.P, M); A(&d.Q, M);
-  A(&d.D, M); A(&d.U, M); A(&d.W, M);
+  A(&d.D, M); A(&d.U, M); A(&d.W, M); A(&d.S, M);
   A(&d.ID, M); A(&d.ID2, M); A(&d.keys, M); A(&d.skeys, M); A(&d.perm, M);
   A(&d.nbr_cnt, M); A(&d.R, M); A(&d.sid, M);
   A(&d.nbr, (size_t)paper_list_words(b->pc.maxn) * M);

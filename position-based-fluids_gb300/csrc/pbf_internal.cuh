@@ -211,6 +211,7 @@ struct DeviceState {
   float4 *D = nullptr;                 // displacement since step start (paper)
   float4 *U = nullptr;                 // velocity and 1/rho (paper)
   float4 *W = nullptr;                 // vorticity and |omega| (paper)
+  float4 *S = nullptr;                 // sum of (1/rho_j) grad W (paper, vorticity pass)
   float *R = nullptr;                  // density (paper)
   // ref-compat: P, V and lambda by sorted slot during the step (P with the
   // Jacobi ping-pong), and the XSPH velocity change by input index

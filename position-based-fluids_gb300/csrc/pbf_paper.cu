@@ -15,10 +15,12 @@
 //   P       predicted position x + d
 //   D       displacement d since the start of the step (kept apart from x so
 //           that positions round once per step, not once per iteration);
-//           the vorticity pass then reuses it for (p, |vorticity|)
-//   Q       (predicted position, lambda) as read by the delta-p pass
+//           the vorticity pass then reuses it for (p, |vorticity| / rho)
+//   Q       (predicted position, lambda) as read by the delta-p pass; the
+//           vorticity pass then reuses it for the XSPH sum
 //   U       (velocity, 1/rho) as read by the velocity passes
 //   W       (vorticity, |vorticity|)
+//   S       sum of (1/rho_j) grad W over the neighbours (vorticity pass)
 // Neighbour sets are built once per step from the predicted positions
 // (Algorithm 1 line 6): N_k = { j != k : r0 <= |p_k - p_j| < h } over the
 // 27 cells around k's cell, r0 = sqrt(FLT_MIN) ~ 1.1e-19 (closer particles
@@ -200,42 +202,40 @@ __global__ void __launch_bounds__(kBlock)
   delta_commit(k, acc, nc, c, D, P, R, U, last);
 }
 
-// Vorticity omega_k; also writes (p_k, |omega_k|) into PW for the next pass.
+// Vorticity pass: omega_k and the sums the XSPH pass uses (pbf_paper.cuh).
 template <int kBlock, int kBatch>
 __global__ void __launch_bounds__(kBlock)
     k_vorticity(const float4 *__restrict__ P, const float4 *__restrict__ U,
                 NbrCtx nc, PaperConsts c, float4 *__restrict__ Wo,
-                float4 *__restrict__ PW) {
+                float4 *__restrict__ PW, float4 *__restrict__ XS, float4 *__restrict__ SS) {
   const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
   if (k >= c.n) return;
   const float4 pk = P[k];
   const float4 uk = U[k];
-  VortAcc acc{0.f, 0.f, 0.f};
+  VortAcc acc{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   visit_neighbours<kBatch>(
       nc, k, [&](uint32_t j) { return PU{__ldg(&P[j]), __ldg(&U[j])}; },
       [&](const PU &d) { acc.pair(pk, uk, d, c); });
-  vort_commit(k, pk, acc, Wo, PW);
+  vort_commit(k, pk, uk, acc, Wo, PW, XS, SS);
 }
 
-// At least 1024 resident threads per SM (64 registers): no spills in any
-// shape.  Left to itself the compiler takes more (96 with eight loads in
-// flight) and halves the resident warps.
+// XSPH + commit: gathers (p_j, |omega_j|/rho_j) only.
 template <int kBlock, int kBatch>
-__global__ void __launch_bounds__(kBlock, 1024 / kBlock)
+__global__ void __launch_bounds__(kBlock)
     k_xsph_commit(const float4 *__restrict__ PW, const float4 *__restrict__ U,
-                  const float4 *__restrict__ Wv, NbrCtx nc, PaperConsts c,
+                  const float4 *__restrict__ Wv, const float4 *__restrict__ XS,
+                  const float4 *__restrict__ SS, NbrCtx nc, PaperConsts c,
                   const uint32_t *__restrict__ ID2, float4 *__restrict__ X,
                   float4 *__restrict__ V, uint32_t *__restrict__ ID) {
   const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
   if (k >= c.n) return;
   const float4 pk = PW[k];
-  const float4 uk = U[k];
-  const float4 wk = load_own(&Wv[k]);
-  XsphAcc acc{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  XsphAcc acc{0.f, 0.f, 0.f};
   visit_neighbours<kBatch>(
-      nc, k, [&](uint32_t j) { return PU{__ldg(&PW[j]), __ldg(&U[j])}; },
-      [&](const PU &d) { acc.pair(pk, uk, wk, d, c); });
-  xsph_commit(k, pk, uk, wk, acc, nc, c, ID2, X, V, ID);
+      nc, k, [&](uint32_t j) { return __ldg(&PW[j]); },
+      [&](const float4 &pj) { acc.pair(pk, pj, c); });
+  xsph_commit(k, pk, load_own(&U[k]), load_own(&Wv[k]), load_own(&XS[k]), load_own(&SS[k]), acc,
+              nc, c, ID2, X, V, ID);
 }
 
 __global__ void k_gather_out(const float4 *__restrict__ X,
@@ -391,13 +391,14 @@ cudaError_t paper_delta(const DeviceState &d, const PaperConsts &c,
 
 cudaError_t paper_vorticity(const DeviceState &d, const PaperConsts &c,
                             const uint16_t *sid, cudaStream_t st) {
-  PBF_GATHER_LAUNCH(k_vorticity, kKindVorticity, d.P, d.U, make_ctx(d, c, sid), c, d.W, d.D);
+  PBF_GATHER_LAUNCH(k_vorticity, kKindVorticity, d.P, d.U, make_ctx(d, c, sid), c, d.W, d.D, d.Q,
+                    d.S);
   return cudaGetLastError();
 }
 
 cudaError_t paper_xsph_commit(const DeviceState &d, const PaperConsts &c,
                               const uint16_t *sid, cudaStream_t st) {
-  PBF_GATHER_LAUNCH(k_xsph_commit, kKindXsph, d.D, d.U, d.W, make_ctx(d, c, sid), c, d.ID2,
+  PBF_GATHER_LAUNCH(k_xsph_commit, kKindXsph, d.D, d.U, d.W, d.Q, d.S, make_ctx(d, c, sid), c, d.ID2,
                     d.X, d.V, d.ID);
   return cudaGetLastError();
 }

@@ -255,7 +255,7 @@ __device__ __forceinline__ float scorr_term(float r2, const PaperConsts &c) {
 __device__ __forceinline__ float spiky_factor(float r2, const PaperConsts &c) {
   float rinv;
   asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(rinv) : "f"(r2));
-  const float hr = __fsub_rn(c.h, __fmul_rn(r2, rinv));
+  const float hr = __fmaf_rn(-r2, rinv, c.h);  // h - r, one rounding (r close to h cancels)
   return __fmul_rn(__fmul_rn(__fmul_rn(-c.spiky, hr), hr), rinv);
 }
 
@@ -268,7 +268,8 @@ __device__ __forceinline__ float poly6_value(float r2, const PaperConsts &c) {
 struct LambdaAcc {
   float rho, gx, gy, gz, s;
   __device__ __forceinline__ void add(const Sep &r, const PaperConsts &c) {
-    rho = __fadd_rn(rho, poly6_value(r.r2, c));
+    const float t = __fsub_rn(c.h2, r.r2);
+    rho = __fmaf_rn(__fmul_rn(__fmul_rn(c.poly6, t), t), t, rho);
     const float f = spiky_factor(r.r2, c);
     gx = __fmaf_rn(f, r.x, gx);
     gy = __fmaf_rn(f, r.y, gy);
@@ -412,9 +413,17 @@ __device__ __forceinline__ float cross_component(float a1, float b2, float a2, f
   return __fmaf_rn(a1, b2, __fmul_rn(-a2, b1));  // a1 b2 - a2 b1
 }
 
-// Vorticity pass: omega_k = sum (1/rho_j) grad W x (v_j - v_k).
+// Vorticity pass, which also carries the neighbour sums the XSPH pass would
+// otherwise gather velocities for:
+//   omega_k = sum (1/rho_j) grad W x (v_j - v_k),
+//   S_k     = sum (1/rho_j) grad W,
+//   X_k     = sum (1/rho_j) W (v_j - v_k)   (XSPH viscosity).
+// With |omega_j| / rho_j gathered in the next pass, the vorticity location
+// vector eta_k = sum (1/rho_j)(|omega_j| - |omega_k|) grad W is
+// sum (|omega_j|/rho_j) grad W - |omega_k| S_k, so that pass gathers one
+// float4 per neighbour instead of two.
 struct VortAcc {
-  float wx, wy, wz;
+  float wx, wy, wz, sx, sy, sz, xx, xy, xz;
   __device__ __forceinline__ void pair(const float4 &pk, const float4 &uk, const PU &d,
                                        const PaperConsts &c) {
     const Sep r = separation(pk, d.p);
@@ -427,62 +436,71 @@ struct VortAcc {
       wx = __fadd_rn(wx, cross_component(gy, uz, gz, uy));
       wy = __fadd_rn(wy, cross_component(gz, ux, gx, uz));
       wz = __fadd_rn(wz, cross_component(gx, uy, gy, ux));
+      sx = __fadd_rn(sx, gx);
+      sy = __fadd_rn(sy, gy);
+      sz = __fadd_rn(sz, gz);
+      const float wp = __fmul_rn(poly6_value(r.r2, c), uj.w);
+      xx = __fmaf_rn(wp, ux, xx);
+      xy = __fmaf_rn(wp, uy, xy);
+      xz = __fmaf_rn(wp, uz, xz);
     }
   }
 };
 __device__ __forceinline__ float norm3(float x, float y, float z) {
   return __fsqrt_rn(__fmaf_rn(z, z, __fmaf_rn(y, y, __fmul_rn(x, x))));
 }
-// Writes omega_k with |omega_k|, and (p_k, |omega_k|) for the XSPH pass.
-__device__ __forceinline__ void vort_commit(uint32_t k, const float4 &pk, const VortAcc &a,
-                                            float4 *__restrict__ Wo, float4 *__restrict__ PW) {
+// Writes (omega_k, |omega_k|), (p_k, |omega_k| / rho_k) for the XSPH pass to
+// gather, and k's own sums X_k and S_k.
+__device__ __forceinline__ void vort_commit(uint32_t k, const float4 &pk, const float4 &uk,
+                                            const VortAcc &a, float4 *__restrict__ Wo,
+                                            float4 *__restrict__ PW, float4 *__restrict__ XS,
+                                            float4 *__restrict__ SS) {
   const float wn = norm3(a.wx, a.wy, a.wz);
   Wo[k] = make_float4(a.wx, a.wy, a.wz, wn);
-  PW[k] = make_float4(pk.x, pk.y, pk.z, wn);
+  PW[k] = make_float4(pk.x, pk.y, pk.z, __fmul_rn(wn, uk.w));
+  XS[k] = make_float4(a.xx, a.xy, a.xz, 0.0f);
+  SS[k] = make_float4(a.sx, a.sy, a.sz, 0.0f);
 }
 
-// XSPH + vorticity-confinement pass: eta = sum (1/rho_j)(|omega_j| -
-// |omega_k|) grad W, and the XSPH sum (1/rho_j)(v_j - v_k) W.
+// XSPH + vorticity-confinement pass: E_k = sum (|omega_j|/rho_j) grad W over
+// the pairs (pj.w = |omega_j|/rho_j).
 struct XsphAcc {
-  float ex, ey, ez, xx, xy, xz;
-  __device__ __forceinline__ void pair(const float4 &pk, const float4 &uk, const float4 &wk,
-                                       const PU &d, const PaperConsts &c) {
-    const float4 pj = d.p;
+  float ex, ey, ez;
+  __device__ __forceinline__ void pair(const float4 &pk, const float4 &pj, const PaperConsts &c) {
     const Sep r = separation(pk, pj);
     if (is_pair(r.r2, c.h2)) {
-      const float4 uj = d.u;
-      const float e = __fmul_rn(__fmul_rn(spiky_factor(r.r2, c), uj.w), __fsub_rn(pj.w, wk.w));
+      const float e = __fmul_rn(spiky_factor(r.r2, c), pj.w);
       ex = __fmaf_rn(e, r.x, ex);
       ey = __fmaf_rn(e, r.y, ey);
       ez = __fmaf_rn(e, r.z, ez);
-      const float wp = __fmul_rn(poly6_value(r.r2, c), uj.w);
-      xx = __fmaf_rn(wp, __fsub_rn(uj.x, uk.x), xx);
-      xy = __fmaf_rn(wp, __fsub_rn(uj.y, uk.y), xy);
-      xz = __fmaf_rn(wp, __fsub_rn(uj.z, uk.z), xz);
     }
   }
 };
-// v = v + dt f_vorticity + c_xsph sum; commits x (.w = |v|), v (.w = mass)
+// eta = E - |omega_k| S_k; v = v + dt f_vorticity + c_xsph X_k with
+// f_vorticity = eps (eta/|eta|) x omega; commits x (.w = |v|), v (.w = mass)
 // and the input index of slot k.
 __device__ __forceinline__ void xsph_commit(uint32_t k, const float4 &pk, const float4 &uk,
-                                            const float4 &wk, const XsphAcc &a, const NbrCtx &nc,
+                                            const float4 &wk, const float4 &xs, const float4 &ss,
+                                            const XsphAcc &a, const NbrCtx &nc,
                                             const PaperConsts &c, const uint32_t *__restrict__ ID2,
                                             float4 *__restrict__ X, float4 *__restrict__ V,
                                             uint32_t *__restrict__ ID) {
-  const float el2 = __fmaf_rn(a.ez, a.ez, __fmaf_rn(a.ey, a.ey, __fmul_rn(a.ex, a.ex)));
+  const float ex = __fmaf_rn(-wk.w, ss.x, a.ex), ey = __fmaf_rn(-wk.w, ss.y, a.ey),
+              ez = __fmaf_rn(-wk.w, ss.z, a.ez);
+  const float el2 = __fmaf_rn(ez, ez, __fmaf_rn(ey, ey, __fmul_rn(ex, ex)));
   float nx = 0.f, ny = 0.f, nz = 0.f;
   if (el2 > 0.0f) {
     const float inv = rsqrtf(el2);
-    nx = __fmul_rn(a.ex, inv);
-    ny = __fmul_rn(a.ey, inv);
-    nz = __fmul_rn(a.ez, inv);
+    nx = __fmul_rn(ex, inv);
+    ny = __fmul_rn(ey, inv);
+    nz = __fmul_rn(ez, inv);
   }
   const float fx = __fmul_rn(c.vort_eps, cross_component(ny, wk.z, nz, wk.y));
   const float fy = __fmul_rn(c.vort_eps, cross_component(nz, wk.x, nx, wk.z));
   const float fz = __fmul_rn(c.vort_eps, cross_component(nx, wk.y, ny, wk.x));
-  const float vx = __fmaf_rn(c.xsph_c, a.xx, __fmaf_rn(c.dt, fx, uk.x));
-  const float vy = __fmaf_rn(c.xsph_c, a.xy, __fmaf_rn(c.dt, fy, uk.y));
-  const float vz = __fmaf_rn(c.xsph_c, a.xz, __fmaf_rn(c.dt, fz, uk.z));
+  const float vx = __fmaf_rn(c.xsph_c, xs.x, __fmaf_rn(c.dt, fx, uk.x));
+  const float vy = __fmaf_rn(c.xsph_c, xs.y, __fmaf_rn(c.dt, fy, uk.y));
+  const float vz = __fmaf_rn(c.xsph_c, xs.z, __fmaf_rn(c.dt, fz, uk.z));
   X[k] = make_float4(pk.x, pk.y, pk.z, norm3(vx, vy, vz));
   V[k] = make_float4(vx, vy, vz, load_own(&nc.V2[k]).w);
   ID[k] = load_own(&ID2[k]);

@@ -413,6 +413,7 @@ int pbf_init(pbf_sim *s) {
     A(&d.D, n);
     A(&d.U, n);
     A(&d.W, n);
+    A(&d.S, n);
     A(&d.R, n);
     A(&d.nbr_cnt, n);
     A(&d.nbr_max, 1);

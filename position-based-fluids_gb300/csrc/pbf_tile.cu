@@ -517,7 +517,8 @@ __global__ void __launch_bounds__(kThreads, kCtasOne)
 
 __global__ void __launch_bounds__(kThreads, kCtasTwo)
     k_vorticity_tile(const float4 *__restrict__ P, const float4 *__restrict__ U, NbrCtx nc,
-                     BlockCtx bc, PaperConsts c, float4 *__restrict__ Wo, float4 *__restrict__ PW) {
+                     BlockCtx bc, PaperConsts c, float4 *__restrict__ Wo, float4 *__restrict__ PW,
+                     float4 *__restrict__ XS, float4 *__restrict__ SS) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const BlockSmem sm{smem_raw};
   const float4 *const src[2] = {P, U};
@@ -526,7 +527,7 @@ __global__ void __launch_bounds__(kThreads, kCtasTwo)
   for_each_block<2>(nc, bc, src, sm, [&](uint32_t k, uint32_t, bool staged) {
     const float4 pk = load_own(&P[k]);
     const float4 uk = load_own(&U[k]);
-    VortAcc acc{0.f, 0.f, 0.f};
+    VortAcc acc{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     const auto pair = [&](const PU &d) { acc.pair(pk, uk, d, c); };
     if (staged) {
       const uint32_t cnt = load_own(&nc.cnt[k]);
@@ -538,37 +539,35 @@ __global__ void __launch_bounds__(kThreads, kCtasTwo)
       visit_neighbours<4>(nc, k, [&](uint32_t j) { return PU{__ldg(&P[j]), __ldg(&U[j])}; },
                           pair);
     }
-    vort_commit(k, pk, acc, Wo, PW);
+    vort_commit(k, pk, uk, acc, Wo, PW, XS, SS);
   });
 }
 
-__global__ void __launch_bounds__(kThreads, kCtasTwo)
+__global__ void __launch_bounds__(kThreads, kCtasOne)
     k_xsph_commit_tile(const float4 *__restrict__ PW, const float4 *__restrict__ U,
-                       const float4 *__restrict__ Wv, NbrCtx nc, BlockCtx bc, PaperConsts c,
+                       const float4 *__restrict__ Wv, const float4 *__restrict__ XS,
+                       const float4 *__restrict__ SS, NbrCtx nc, BlockCtx bc, PaperConsts c,
                        const uint32_t *__restrict__ ID2, float4 *__restrict__ X,
                        float4 *__restrict__ V, uint32_t *__restrict__ ID) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const BlockSmem sm{smem_raw};
-  const float4 *const src[2] = {PW, U};
+  const float4 *const src[1] = {PW};
   const float4 *__restrict__ sp = sm.stage(0);
-  const float4 *__restrict__ su = sm.stage(1);
-  for_each_block<2>(nc, bc, src, sm, [&](uint32_t k, uint32_t, bool staged) {
+  for_each_block<1>(nc, bc, src, sm, [&](uint32_t k, uint32_t, bool staged) {
     const float4 pk = load_own(&PW[k]);
-    const float4 uk = load_own(&U[k]);
-    const float4 wk = load_own(&Wv[k]);
-    XsphAcc acc{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    const auto pair = [&](const PU &d) { acc.pair(pk, uk, wk, d, c); };
+    XsphAcc acc{0.f, 0.f, 0.f};
+    const auto pair = [&](const float4 &pj) { acc.pair(pk, pj, c); };
     if (staged) {
       const uint32_t cnt = load_own(&nc.cnt[k]);
       if (cnt <= c.maxn)
-        for_each_staged(nc, k, cnt, [&](uint32_t i) { return PU{sp[i], su[i]}; }, pair);
+        for_each_staged(nc, k, cnt, [&](uint32_t i) { return sp[i]; }, pair);
       else
-        visit_fallback(nc, k, [&](uint32_t j) { pair(PU{__ldg(&PW[j]), __ldg(&U[j])}); });
+        visit_fallback(nc, k, [&](uint32_t j) { pair(__ldg(&PW[j])); });
     } else {
-      visit_neighbours<4>(nc, k, [&](uint32_t j) { return PU{__ldg(&PW[j]), __ldg(&U[j])}; },
-                          pair);
+      visit_neighbours<4>(nc, k, [&](uint32_t j) { return __ldg(&PW[j]); }, pair);
     }
-    xsph_commit(k, pk, uk, wk, acc, nc, c, ID2, X, V, ID);
+    xsph_commit(k, pk, load_own(&U[k]), load_own(&Wv[k]), load_own(&XS[k]), load_own(&SS[k]), acc,
+                nc, c, ID2, X, V, ID);
   });
 }
 
@@ -619,7 +618,7 @@ void init_kernels() {
   if (e == cudaSuccess) e = fit(k_lambda_tile, 1, &one);
   if (e == cudaSuccess) e = fit(k_delta_tile, 1, &one);
   if (e == cudaSuccess) e = fit(k_vorticity_tile, 2, &two);
-  if (e == cudaSuccess) e = fit(k_xsph_commit_tile, 2, &two);
+  if (e == cudaSuccess) e = fit(k_xsph_commit_tile, 1, &one);
   if (e == cudaSuccess) {
     g_grid_one = (uint32_t)(std::max(1, one) * sms);
     g_grid_two = (uint32_t)(std::max(1, two) * sms);
@@ -684,13 +683,13 @@ cudaError_t tile_delta(const DeviceState &d, const PaperConsts &c, const uint16_
 cudaError_t tile_vorticity(const DeviceState &d, const PaperConsts &c, const uint16_t *sid,
                            uint32_t nscenes, cudaStream_t st) {
   PBF_BLOCK_LAUNCH(k_vorticity_tile, kKindVorticity, 2, d.P, d.U, make_ctx(d, c, sid),
-                   make_blocks(d, nscenes), c, d.W, d.D);
+                   make_blocks(d, nscenes), c, d.W, d.D, d.Q, d.S);
   return cudaGetLastError();
 }
 
 cudaError_t tile_xsph_commit(const DeviceState &d, const PaperConsts &c, const uint16_t *sid,
                              uint32_t nscenes, cudaStream_t st) {
-  PBF_BLOCK_LAUNCH(k_xsph_commit_tile, kKindXsph, 2, d.D, d.U, d.W, make_ctx(d, c, sid),
+  PBF_BLOCK_LAUNCH(k_xsph_commit_tile, kKindXsph, 1, d.D, d.U, d.W, d.Q, d.S, make_ctx(d, c, sid),
                    make_blocks(d, nscenes), c, d.ID2, d.X, d.V, d.ID);
   return cudaGetLastError();
 }
