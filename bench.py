@@ -92,19 +92,39 @@ ITERATIONS = 4
 METRIC = "particle-iterations/s"
 UNIT = "particle-iterations/s"
 # Compulsory HBM bytes per particle and launch of each stage (neighbour
-# re-reads counted as cache hits): predict+hash 72, sort 52 (18-bit keys),
-# cell ranges 8, reorder 104, lambda 24, delta-p 36, vorticity 48,
-# XSPH+commit 84; 608 per particle-step in total.  The neighbour-list build
-# (read p* 16, write the count 4) is an implementation choice outside that
-# total; fused with the first lambda it counts both (20 + 24).  Every kernel
-# the step launches has an entry, so the roofline object names the kernel
-# that takes the most time.
+# re-reads counted as cache hits): predict+hash 72, sort 4 + 16 per digit
+# pass (36 for the 18-bit keys of a 64^3 grid: two 9-bit passes), cell
+# ranges 8, reorder 104, lambda 24, delta-p 36, vorticity 48, XSPH+commit 84;
+# 556 + the sort per particle-step in total (592 on a 64^3 grid).  The
+# neighbour-list build (read p* 16, write the count 4) is an implementation
+# choice outside that total; fused with the first lambda it counts both
+# (20 + 24).  Every kernel the step launches has an entry, so the roofline
+# object names the kernel that takes the most time.
 ALG_BYTES = {
-    "predict_hash": 72, "sort_onesweep": 52, "cell_offsets": 8, "reorder": 104,
+    "predict_hash": 72, "sort_onesweep": 36, "cell_offsets": 8, "reorder": 104,
     "nbr_build": 20, "nbr_lambda": 44, "lambda": 24, "delta": 36, "vorticity": 48,
     "xsph_commit": 84,
 }
-STEP_BYTES = 608
+STEP_BYTES_BUT_SORT = 556
+
+
+def sort_passes(key_bits: int) -> int:
+    """Digit passes of the radix sort: 9-bit digits for 9 and 17-18 key bits
+    (where they save a pass within two passes), 8-bit ones otherwise."""
+    w = 9 if key_bits in (9, 17, 18) else 8
+    return -(-key_bits // w)
+
+
+def sort_key_bits(cells: int) -> int:
+    return max(1, int(np.ceil(np.log2(max(cells, 2)))))
+
+
+def sort_bytes(cells: int) -> int:
+    return 4 + 16 * sort_passes(sort_key_bits(cells))
+
+
+def step_bytes(cells: int) -> int:
+    return STEP_BYTES_BUT_SORT + sort_bytes(cells)
 
 
 def measured_peaks() -> dict:
@@ -458,6 +478,9 @@ def run_ours(args) -> int:
 
     # warm-up (also instantiates the step graph)
     sim.step(args.warmup)
+    # the state the timed steps start from: the per-kernel timing pass below
+    # replays the same steps from it
+    start_state = sim.dumpData()
 
     # ---- device-resident throughput ------------------------------------
     with ClockSampler(local) as clocks:
@@ -502,9 +525,11 @@ def run_ours(args) -> int:
     hp.pbf_host_free(pin_pos)
     hp.pbf_host_free(pin_vel)
 
-    # ---- per-kernel timing pass (events after every launch) -------------
+    # ---- per-kernel timing pass: the timed steps again, from the same ----
+    # state, with an event after every launch (each step one graph)
+    sim.set_state(*start_state)
     sim.set_stage_timing(True)
-    kt_steps = max(3, min(args.steps, 10))
+    kt_steps = args.steps
     sim.step(kt_steps)
     kt = sim.kernel_times()
     stages = sim.stage_times()
@@ -516,19 +541,21 @@ def run_ours(args) -> int:
     if dom == "sort_onesweep":
         per_launch_s = dom_ms / 1e3 / kt_steps
     peaks = measured_peaks()
-    achieved = ALG_BYTES[dom] * n / per_launch_s / 1e9
+    alg = dict(ALG_BYTES, sort_onesweep=sort_bytes(sc.params.ncells))
+    achieved = alg[dom] * n / per_launch_s / 1e9
     traffic = profile_traffic(dom)
     roofline = {
         "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
         "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
         "traffic": (traffic[0] * n / traffic[1]) if traffic else None,
-        "algorithmic_bytes_per_launch": ALG_BYTES[dom] * n,
+        "algorithmic_bytes_per_launch": alg[dom] * n,
         "avg_launch_ms": per_launch_s * 1e3, "share_of_step": dom_ms / total_ms,
     }
     step_s = t_dev / args.steps
-    step_roofline = {"bytes_per_particle_step": STEP_BYTES,
-                     "achieved_gbs": STEP_BYTES * n / step_s / 1e9,
-                     "frac": STEP_BYTES * n / step_s / 1e9 / peaks["hbm_gbs"]}
+    sb = step_bytes(sc.params.ncells)
+    step_roofline = {"bytes_per_particle_step": sb,
+                     "achieved_gbs": sb * n / step_s / 1e9,
+                     "frac": sb * n / step_s / 1e9 / peaks["hbm_gbs"]}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -559,6 +586,9 @@ def run_ours(args) -> int:
             "stage_ms": {"sort": float(stages[0]), "lambda": float(stages[1]), "delta_p": float(stages[2]),
                          "velocity": float(stages[3])},
             "kernel_ms_per_step": {k: v[0] / kt_steps for k, v in kt.items()},
+            "kernel_timing": {"steps": kt_steps, "sum_ms_per_step": total_ms / kt_steps,
+                              "method": "the timed steps replayed from their start state, each "
+                                        "step one graph with an event after every launch"},
             "clocks": clock_summary,
             "density_error": density_error,
             "fp64_step_error": fp64_err,
@@ -654,9 +684,8 @@ def run_batch(args, emit: bool = True):
     t_wall = reduce_max(dist, t_wall, device="cuda")
     e2e_value = world * work_e2e / t_wall
     peaks = measured_peaks()
-    sort_bits = int(np.ceil(np.log2(max(cells_tot, 2))))
-    step_bytes = STEP_BYTES - 52 + 4 + 16 * ((sort_bits + 7) // 8)
-    step_gbs = step_bytes * n_tot / (t_dev / steps) / 1e9
+    batch_step_bytes = step_bytes(cells_tot)
+    step_gbs = batch_step_bytes * n_tot / (t_dev / steps) / 1e9
 
     # ---- the same scenes one by one on the plain path ---------------------
     plain = None
@@ -689,7 +718,7 @@ def run_batch(args, emit: bool = True):
                               f"{args.warmup}+{steps} steps and read-back of every scene",
                     "finite": finite},
             "gpu_launches": launches * steps,
-            "step_roofline": {"bytes_per_particle_step": step_bytes, "achieved_gbs": step_gbs,
+            "step_roofline": {"bytes_per_particle_step": batch_step_bytes, "achieved_gbs": step_gbs,
                               "frac": step_gbs / peaks["hbm_gbs"], "peak_source": peaks["source"]},
             "scene_latency_s": {"p50": t_wall, "p99": t_wall,
                                 "note": "every scene of the batch completes with the last step"},

@@ -219,12 +219,11 @@ size_t pbf_batch_device_bytes(const pbf_params *solver, uint32_t max_scenes,
                               uint32_t max_particles, uint32_t max_cells) {
   if (!solver) return 0;
   const PaperConsts pc = make_paper_consts(*solver, max_particles);
-  const SortPlan plan = make_sort_plan(max_particles, 32);
   return (size_t)max_particles * bytes_per_particle(pc.maxn) +
          ((size_t)max_cells + 1) * sizeof(uint32_t) +
          (size_t)max_cells * sizeof(uint32_t) + 3 * sizeof(uint32_t) +  // cell-block list
          (size_t)offset_runs_capacity(max_cells) * sizeof(uint4) + sizeof(uint32_t) +
-         plan.words * sizeof(uint32_t) +
+         sort_words_max(max_particles) * sizeof(uint32_t) +
          (size_t)max_scenes * sizeof(SceneDesc) + 64;
 }
 
@@ -274,7 +273,7 @@ int pbf_batch_create(const pbf_params *solver, uint32_t max_scenes, uint32_t max
   A(&d.offsets, (size_t)max_cells + 1);
   A(&d.runs, offset_runs_capacity(max_cells));
   A(&d.runs_count, 1);
-  A(&d.sort_scratch, make_sort_plan(max_particles, 32).words);
+  A(&d.sort_scratch, sort_words_max(max_particles));
   A(&d.scenes, max_scenes);
   A(&d.err, 1);
   if (rc == PBF_OK) {

@@ -21,17 +21,19 @@ __device__ __forceinline__ uint32_t scene_cell(float x, float y, float z,
          (uint32_t)s.ncell[0] * ((uint32_t)cy + (uint32_t)s.ncell[1] * (uint32_t)cz);
 }
 
-// Accumulates the per-pass digit histograms of one key per lane into
-// shared memory, aggregating equal digits within the warp first.
+// Accumulates the per-pass digit histograms (digit_bits wide, pass p's
+// histogram at p << digit_bits) of one key per lane into shared memory,
+// aggregating equal digits within the warp first.
 __device__ __forceinline__ void warp_digit_histogram(uint32_t key, bool valid,
-                                                     uint32_t passes,
+                                                     uint32_t passes, uint32_t digit_bits,
                                                      uint32_t *s_hist) {
   const unsigned lane = threadIdx.x & 31u;
+  const uint32_t mask = (1u << digit_bits) - 1u;
   for (uint32_t p = 0; p < passes; ++p) {
-    const uint32_t d = (key >> (p * kRadixBits)) & (kRadix - 1);
+    const uint32_t d = (key >> (p * digit_bits)) & mask;
     const unsigned peers = __match_any_sync(0xffffffffu, valid ? d : 0xffffffffu);
     if (valid && lane == (unsigned)(__ffs(peers) - 1))
-      atomicAdd(&s_hist[p * kRadix + d], (uint32_t)__popc(peers));
+      atomicAdd(&s_hist[(p << digit_bits) + d], (uint32_t)__popc(peers));
   }
 }
 

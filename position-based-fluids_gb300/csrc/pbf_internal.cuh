@@ -61,26 +61,78 @@ struct RefConsts {
 constexpr uint32_t kStrideCtas = 152u * 8u;
 
 // ------------------------------------------------------------------ sort --
-constexpr int kRadixBits = 8;
-constexpr int kRadix = 1 << kRadixBits;
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr int kMaxSortPasses = 4;
+// Digit widths: 8 bits (one digit per scan thread) or 9 bits (two).
+constexpr uint32_t kMinDigitBits = 8;
+constexpr uint32_t kMaxDigitBits = 9;
+// passes * radix of any plan (four 8-bit passes, two 9-bit ones)
+constexpr uint32_t kMaxHistWords = 1024;
+// Words of the look-back wait self-test: two tiles of 8-bit digits + flag.
+constexpr uint32_t kSelftestWords = 2u * (1u << kMinDigitBits) + 1u;
+
+// 9-bit digits where they save a pass within two passes -- 9-bit keys (one
+// pass instead of two) and 17-18-bit keys (two instead of three, e.g. the
+// cells of a 64^3 grid) -- and 8-bit digits otherwise.  On GB300 a 9-bit
+// pass costs about 1.4 times an 8-bit one: two of them beat three 8-bit
+// passes, three do not beat four, and 10-bit passes lost to 8-bit ones.
+constexpr uint32_t sort_digit_bits_for(uint32_t key_bits) {
+  return (key_bits == 9 || key_bits == 17 || key_bits == 18) ? 9u : 8u;
+}
+constexpr uint32_t sort_passes_for(uint32_t key_bits) {
+  const uint32_t w = sort_digit_bits_for(key_bits);
+  return (key_bits + w - 1) / w;
+}
 
 // Layout of the radix-sort scratch inside one allocation (32-bit words).
 struct SortPlan {
   uint32_t n = 0, key_bits = 0, passes = 0, tiles = 0;
-  size_t off_hist = 0;      // passes * kRadix: digit histograms, then prefixes
+  uint32_t digit_bits = 0, radix = 0;
+  size_t off_hist = 0;      // passes * radix: digit histograms, then prefixes
   size_t off_counter = 0;   // 32 words: per-pass tile counters
-  size_t off_lookback = 0;  // passes * tiles * kRadix
+  size_t off_lookback = 0;  // passes * tiles * radix
   size_t clear_words = 0;   // words from off_hist that must start at zero
   size_t off_keys_alt = 0;  // n
   size_t off_vals_alt = 0;  // n
   size_t words = 0;         // total
 };
 
-SortPlan make_sort_plan(uint32_t n, uint32_t key_bits);
+constexpr SortPlan make_sort_plan(uint32_t n, uint32_t key_bits) {
+  SortPlan p;
+  p.n = n;
+  p.key_bits = key_bits < 1 ? 1 : (key_bits > 32 ? 32 : key_bits);
+  p.passes = sort_passes_for(p.key_bits);
+  p.digit_bits = sort_digit_bits_for(p.key_bits);
+  p.radix = 1u << p.digit_bits;
+  p.tiles = (uint32_t)(((uint64_t)n + kSortTile - 1) / kSortTile);
+  size_t w = 0;
+  p.off_hist = w;
+  w += (size_t)p.passes * p.radix;
+  p.off_counter = w;
+  w += 32;
+  p.off_lookback = w;
+  w += (size_t)p.passes * p.tiles * p.radix;
+  p.clear_words = w - p.off_hist;
+  w = (w + 63) & ~size_t(63);
+  p.off_keys_alt = w;
+  w += (size_t)n;
+  w = (w + 63) & ~size_t(63);
+  p.off_vals_alt = w;
+  w += (size_t)n;
+  p.words = w;
+  return p;
+}
+// The largest scratch (words) a plan of n keys of any width lays out.
+constexpr size_t sort_words_max(uint32_t n) {
+  size_t w = 0;
+  for (uint32_t b = 1; b <= 32; ++b) {
+    const size_t x = make_sort_plan(n, b).words;
+    w = x > w ? x : w;
+  }
+  return w;
+}
 uint32_t bits_for(uint32_t max_key_exclusive);
 
 // Zeroes the histogram/counter/look-back words of `scratch`.
@@ -116,7 +168,8 @@ cudaError_t find_cells(const uint32_t *offsets, uint32_t ncells,
 cudaError_t cell_hash(const float4 *pred, uint32_t n, const SceneDesc &scene,
                       uint32_t *hash, cudaStream_t stream);
 // Runs the sort's bounded look-back wait against a predecessor that never
-// publishes (scratch: 2 * kRadix zeroed words); sets kDevErrLookback in *err
+// publishes (scratch: kSelftestWords zeroed words, the last one the flag);
+// sets kDevErrLookback in *err
 // after spin_limit polls.
 cudaError_t wait_selftest(uint32_t *scratch, uint32_t spin_limit, uint32_t *err,
                           cudaStream_t stream);

@@ -23,17 +23,8 @@ namespace {
 constexpr uint32_t kNoAllocMaxKeys = 1u << 20;
 constexpr int kMaxDevices = 64;
 
-constexpr size_t align64(size_t w) { return (w + 63) & ~size_t(63); }
-// Words make_sort_plan lays out for n keys and the maximum number of passes.
-constexpr size_t words_for(uint32_t n) {
-  const size_t tiles = ((size_t)n + kSortTile - 1) / kSortTile;
-  size_t w = (size_t)kMaxSortPasses * kRadix + 32 +
-             (size_t)kMaxSortPasses * tiles * kRadix;
-  w = align64(w) + n;
-  w = align64(w) + n;
-  return w;
-}
-constexpr size_t kNoAllocWords = words_for(kNoAllocMaxKeys);
+// The largest plan of any key width for the most keys.
+constexpr size_t kNoAllocWords = sort_words_max(kNoAllocMaxKeys);
 
 static __device__ __align__(256) uint32_t g_sort_scratch[kNoAllocWords];
 

@@ -67,9 +67,10 @@ __global__ void __launch_bounds__(256)
                    uint32_t n, PaperConsts c,
                    const SceneDesc *__restrict__ scenes,
                    const uint16_t *__restrict__ sid, uint32_t *__restrict__ keys,
-                   uint32_t passes, uint32_t *__restrict__ hist) {
-  __shared__ uint32_t s_hist[kMaxSortPasses * kRadix];
-  for (uint32_t i = threadIdx.x; i < passes * kRadix; i += blockDim.x) s_hist[i] = 0;
+                   uint32_t passes, uint32_t digit_bits, uint32_t *__restrict__ hist) {
+  __shared__ uint32_t s_hist[kMaxHistWords];
+  const uint32_t hist_words = passes << digit_bits;
+  for (uint32_t i = threadIdx.x; i < hist_words; i += blockDim.x) s_hist[i] = 0;
   __syncthreads();
   // Grid-stride over the particles (whole warps iterate together so that
   // __match_any_sync sees every lane): one histogram flush per CTA.
@@ -86,10 +87,10 @@ __global__ void __launch_bounds__(256)
       key = s.cell_base + scene_cell(p.x, p.y, p.z, s);
       keys[k] = key;
     }
-    warp_digit_histogram(key, valid, passes, s_hist);
+    warp_digit_histogram(key, valid, passes, digit_bits, s_hist);
   }
   __syncthreads();
-  for (uint32_t i = threadIdx.x; i < passes * kRadix; i += blockDim.x)
+  for (uint32_t i = threadIdx.x; i < hist_words; i += blockDim.x)
     if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
 }
 
@@ -320,7 +321,8 @@ cudaError_t paper_predict_hash(const float4 *X, const float4 *V, uint32_t n,
                                const SortPlan &plan, uint32_t *sort_scratch,
                                cudaStream_t st) {
   k_predict_hash<<<min(blocks_for(n, 256), kStrideCtas), 256, 0, st>>>(
-      X, V, n, c, scenes, sid, keys, plan.passes, sort_scratch + plan.off_hist);
+      X, V, n, c, scenes, sid, keys, plan.passes, plan.digit_bits,
+      sort_scratch + plan.off_hist);
   return cudaGetLastError();
 }
 

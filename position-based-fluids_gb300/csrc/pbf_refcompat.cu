@@ -67,9 +67,10 @@ __global__ void __launch_bounds__(256)
                       float4 *__restrict__ P, uint32_t n, RefConsts k,
                       const SceneDesc *__restrict__ scenes,
                       uint32_t *__restrict__ keys, uint32_t passes,
-                      uint32_t *__restrict__ hist) {
-  __shared__ uint32_t s_hist[kMaxSortPasses * kRadix];
-  for (uint32_t t = threadIdx.x; t < passes * kRadix; t += blockDim.x) s_hist[t] = 0;
+                      uint32_t digit_bits, uint32_t *__restrict__ hist) {
+  __shared__ uint32_t s_hist[kMaxHistWords];
+  const uint32_t hist_words = passes << digit_bits;
+  for (uint32_t t = threadIdx.x; t < hist_words; t += blockDim.x) s_hist[t] = 0;
   __syncthreads();
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = i < n;
@@ -89,9 +90,9 @@ __global__ void __launch_bounds__(256)
     key = scene_cell(p.x, p.y, p.z, scenes[0]);
     keys[i] = key;
   }
-  warp_digit_histogram(key, valid, passes, s_hist);
+  warp_digit_histogram(key, valid, passes, digit_bits, s_hist);
   __syncthreads();
-  for (uint32_t t = threadIdx.x; t < passes * kRadix; t += blockDim.x)
+  for (uint32_t t = threadIdx.x; t < hist_words; t += blockDim.x)
     if (s_hist[t]) atomicAdd(&hist[t], s_hist[t]);
 }
 
@@ -246,7 +247,8 @@ cudaError_t rc_predict_hash(float4 *X, float4 *V, float4 *P, uint32_t n,
                             uint32_t *keys, const SortPlan &plan,
                             uint32_t *sort_scratch, cudaStream_t st) {
   k_rc_predict_hash<<<blocks_for(n, 256), 256, 0, st>>>(
-      X, V, P, n, k, scenes, keys, plan.passes, sort_scratch + plan.off_hist);
+      X, V, P, n, k, scenes, keys, plan.passes, plan.digit_bits,
+      sort_scratch + plan.off_hist);
   return cudaGetLastError();
 }
 

@@ -48,8 +48,12 @@ struct pbf_sim {
   // CUDA graph of one step
   bool use_graph = true;
   cudaGraphExec_t graph = nullptr;
-  // per-stage timing
+  // per-stage timing: each timed step is captured (with its boundary events
+  // as event-record nodes) and launched as one graph, so the device runs it
+  // back to back as an untimed step does and host enqueue gaps stay out of
+  // the intervals
   bool timing = false;
+  bool timed_capture = false;
   std::vector<cudaEvent_t> events;
   std::vector<int> event_stage;
   std::vector<const char *> event_name;
@@ -67,6 +71,11 @@ struct pbf_sim {
   // looks at the count of the step two back (the first step's right after
   // it) and grows the lists when it came within 1/8 of the capacity
   uint32_t *nbr_max_host = nullptr;
+  // the copy of that count runs on a side branch of the step (forked after
+  // the list build, joined at the step's end) so the solver passes do not
+  // wait for it
+  cudaStream_t count_stream = nullptr;
+  cudaEvent_t count_fork = nullptr, count_join = nullptr;
   cudaEvent_t step_done[2] = {nullptr, nullptr};
   uint64_t launched = 0;  // steps launched since init or the last growth
   uint32_t list_grows = 0;
@@ -97,6 +106,11 @@ void free_all(pbf_sim *s) {
   }
   if (s->nbr_max_host) cudaFreeHost(s->nbr_max_host);
   s->nbr_max_host = nullptr;
+  if (s->count_fork) cudaEventDestroy(s->count_fork);
+  if (s->count_join) cudaEventDestroy(s->count_join);
+  if (s->count_stream) cudaStreamDestroy(s->count_stream);
+  s->count_fork = s->count_join = nullptr;
+  s->count_stream = nullptr;
   for (cudaEvent_t e : s->events) cudaEventDestroy(e);
   s->events.clear();
   for (void *p : s->allocations) cudaFree(p);
@@ -134,7 +148,10 @@ int mark(pbf_sim *s, int stage, const char *name, uint32_t launches,
   s->event_stage[*next] = stage;
   s->event_name[*next] = name;
   s->event_launches[*next] = launches;
-  PBF_TRY(cudaEventRecord(s->events[*next], s->stream));
+  if (s->timed_capture)
+    PBF_TRY(cudaEventRecordWithFlags(s->events[*next], s->stream, cudaEventRecordExternal));
+  else
+    PBF_TRY(cudaEventRecord(s->events[*next], s->stream));
   ++*next;
   return PBF_OK;
 }
@@ -144,6 +161,23 @@ cudaError_t step_offsets(pbf_sim *s) {
   if (s->offset_runs)
     return cell_offsets_runs(d.skeys, s->n, s->ncells, d.offsets, d.runs, d.runs_count, s->stream);
   return cell_offsets(d.skeys, s->n, s->ncells, d.offsets, s->stream);
+}
+
+// Copies the step's largest neighbour count (complete once the list build
+// has run) to page-locked host memory on the side stream; join_count_copy
+// at the end of the step makes the step wait for it.
+cudaError_t fork_count_copy(pbf_sim *s) {
+  cudaError_t e = cudaEventRecord(s->count_fork, s->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s->count_stream, s->count_fork, 0);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->nbr_max_host, s->d.nbr_max, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                        s->count_stream);
+  if (e == cudaSuccess) e = cudaEventRecord(s->count_join, s->count_stream);
+  return e;
+}
+
+cudaError_t join_count_copy(pbf_sim *s) {
+  return cudaStreamWaitEvent(s->stream, s->count_join, 0);
 }
 
 int launch_step(pbf_sim *s) {
@@ -156,6 +190,7 @@ int launch_step(pbf_sim *s) {
   PBF_TRY_STATUS(mark(s, -1, "start", 0, &ev));
   PBF_TRY(sort_clear(s->plan, d.sort_scratch, st));
   if (s->paper) {
+    PBF_TRY(cudaMemsetAsync(d.nbr_max, 0, sizeof(uint32_t), st));
     PBF_TRY(paper_predict_hash(d.X, d.V, n, s->pc, d.scenes, nullptr, d.keys,
                                s->plan, d.sort_scratch, st));
     PBF_TRY_STATUS(mark(s, 0, "predict_hash", 1, &ev));
@@ -169,15 +204,13 @@ int launch_step(pbf_sim *s) {
                           d.P, d.D, st));
     PBF_TRY_STATUS(mark(s, 0, "reorder", 1, &ev));
     const uint32_t iters = s->prm.solver_iterations;
-    PBF_TRY(cudaMemsetAsync(d.nbr_max, 0, sizeof(uint32_t), st));
     if (d.tune.staged) {
       PBF_TRY(tile_plan(d, s->pc, nullptr, 1, st));
       PBF_TRY_STATUS(mark(s, 0, "tile_plan", 1, &ev));
       for (uint32_t it = 0; it < iters; ++it) {
         if (it == 0) {
           PBF_TRY(tile_nbr_build(d, s->pc, nullptr, 1, st));
-          PBF_TRY(cudaMemcpyAsync(s->nbr_max_host, d.nbr_max, sizeof(uint32_t),
-                                  cudaMemcpyDeviceToHost, st));
+          PBF_TRY(fork_count_copy(s));
           PBF_TRY_STATUS(mark(s, 1, "nbr_build", 1, &ev));
         }
         PBF_TRY(tile_lambda(d, s->pc, nullptr, 1, st));
@@ -189,18 +222,17 @@ int launch_step(pbf_sim *s) {
       PBF_TRY_STATUS(mark(s, 3, "vorticity", 1, &ev));
       PBF_TRY(tile_xsph_commit(d, s->pc, nullptr, 1, st));
       PBF_TRY_STATUS(mark(s, 3, "xsph_commit", 1, &ev));
+      PBF_TRY(join_count_copy(s));
     } else {
       for (uint32_t it = 0; it < iters; ++it) {
         if (it == 0 && d.tune.fuse_first) {
           PBF_TRY(paper_nbr_lambda(d, s->pc, nullptr, st));
-          PBF_TRY(cudaMemcpyAsync(s->nbr_max_host, d.nbr_max, sizeof(uint32_t),
-                                  cudaMemcpyDeviceToHost, st));
+          PBF_TRY(fork_count_copy(s));
           PBF_TRY_STATUS(mark(s, 1, "nbr_lambda", 1, &ev));
         } else {
           if (it == 0) {
             PBF_TRY(paper_nbr_build(d, s->pc, nullptr, st));
-            PBF_TRY(cudaMemcpyAsync(s->nbr_max_host, d.nbr_max, sizeof(uint32_t),
-                                    cudaMemcpyDeviceToHost, st));
+            PBF_TRY(fork_count_copy(s));
             PBF_TRY_STATUS(mark(s, 1, "nbr_build", 1, &ev));
           }
           PBF_TRY(paper_lambda(d, s->pc, nullptr, st));
@@ -213,6 +245,7 @@ int launch_step(pbf_sim *s) {
       PBF_TRY_STATUS(mark(s, 3, "vorticity", 1, &ev));
       PBF_TRY(paper_xsph_commit(d, s->pc, nullptr, st));
       PBF_TRY_STATUS(mark(s, 3, "xsph_commit", 1, &ev));
+      PBF_TRY(join_count_copy(s));
     }
   } else {
     PBF_TRY(rc_predict_hash(d.X, d.V, d.P, n, s->rc, d.scenes, d.keys, s->plan,
@@ -286,6 +319,39 @@ int build_graph(pbf_sim *s) {
     s->graph = nullptr;
     return cuda_status(ie, "cudaGraphInstantiate");
   }
+  return PBF_OK;
+}
+
+// One step with its stage boundaries, captured and launched as a graph.
+int launch_timed_step(pbf_sim *s) {
+  // the boundary events exist before the capture (one per mark of a step:
+  // at most 8 outside the solver loop, 2 per iteration)
+  const size_t marks = 16 + 2 * (size_t)s->prm.solver_iterations;
+  while (s->events.size() < marks) {
+    cudaEvent_t e;
+    PBF_TRY(cudaEventCreate(&e));
+    s->events.push_back(e);
+    s->event_stage.push_back(-1);
+    s->event_name.push_back("");
+    s->event_launches.push_back(0);
+  }
+  cudaGraph_t g = nullptr;
+  PBF_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  s->timed_capture = true;
+  const int rc = launch_step(s);
+  s->timed_capture = false;
+  const cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+  if (rc != PBF_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_status(e, "cudaStreamEndCapture");
+  cudaGraphExec_t x = nullptr;
+  cudaError_t le = cudaGraphInstantiate(&x, g, 0);
+  cudaGraphDestroy(g);
+  if (le == cudaSuccess) le = cudaGraphLaunch(x, s->stream);
+  if (x) cudaGraphExecDestroy(x);  // released once the launch completes
+  if (le != cudaSuccess) return cuda_status(le, "timed step graph");
   return PBF_OK;
 }
 
@@ -433,6 +499,9 @@ int pbf_init(pbf_sim *s) {
     if (te == cudaSuccess) te = cudaMallocHost(&s->nbr_max_host, sizeof(uint32_t));
     for (cudaEvent_t &e : s->step_done)
       if (te == cudaSuccess) te = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (te == cudaSuccess) te = cudaStreamCreateWithFlags(&s->count_stream, cudaStreamNonBlocking);
+    if (te == cudaSuccess) te = cudaEventCreateWithFlags(&s->count_fork, cudaEventDisableTiming);
+    if (te == cudaSuccess) te = cudaEventCreateWithFlags(&s->count_join, cudaEventDisableTiming);
     if (te != cudaSuccess) rc = cuda_status(te, "pbf_init");
     else *s->nbr_max_host = 0;
   }
@@ -470,7 +539,7 @@ int pbf_step(pbf_sim *s, uint32_t nsteps) {
     if (s->scene_dirty) PBF_TRY_STATUS(upload_scene(s));
     PBF_TRY_STATUS(adapt_lists(s));
     if (s->timing) {
-      PBF_TRY_STATUS(launch_step(s));
+      PBF_TRY_STATUS(s->use_graph ? launch_timed_step(s) : launch_step(s));
       PBF_TRY_STATUS(collect_times(s));
     } else if (s->use_graph) {
       PBF_TRY_STATUS(build_graph(s));
@@ -830,10 +899,10 @@ int pbf_selftest_bounded_wait(uint32_t spin_limit, uint32_t *device_flag) {
   };
   *device_flag = 0;
   if (cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "selftest") &&
-      cuda(cudaMalloc(&buf, (2 * kRadix + 1) * sizeof(uint32_t)), "selftest") &&
-      cuda(cudaMemsetAsync(buf, 0, (2 * kRadix + 1) * sizeof(uint32_t), st), "selftest") &&
-      cuda(wait_selftest(buf, spin_limit, buf + 2 * kRadix, st), "selftest") &&
-      cuda(cudaMemcpyAsync(device_flag, buf + 2 * kRadix, sizeof(uint32_t),
+      cuda(cudaMalloc(&buf, kSelftestWords * sizeof(uint32_t)), "selftest") &&
+      cuda(cudaMemsetAsync(buf, 0, kSelftestWords * sizeof(uint32_t), st), "selftest") &&
+      cuda(wait_selftest(buf, spin_limit, buf + kSelftestWords - 1, st), "selftest") &&
+      cuda(cudaMemcpyAsync(device_flag, buf + kSelftestWords - 1, sizeof(uint32_t),
                            cudaMemcpyDeviceToHost, st), "selftest"))
     cuda(cudaStreamSynchronize(st), "selftest");
   if (buf) cudaFree(buf);

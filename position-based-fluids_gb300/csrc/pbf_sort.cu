@@ -13,12 +13,16 @@
 //     of init_cells.cl and find_cells.cl.
 //
 // The sort is the onesweep scheme (one upfront histogram pass for every
-// digit, then one pass per 8-bit digit that ranks a tile of keys with
-// warp-level multisplit, publishes per-digit tile counts and resolves its
-// global offsets by decoupled look-back).  Tiles are numbered by an atomic
+// digit, then one pass per digit that ranks a tile of keys with warp-level
+// multisplit, publishes per-digit tile counts and resolves its global
+// offsets by decoupled look-back).  Digits are 8 bits wide, or 9 where that
+// saves a pass within two passes: the 18-bit cell keys of a 64^3-cell grid
+// take two 9-bit passes instead of three 8-bit ones.  Tiles are numbered by an atomic
 // counter in the order CTAs start, so a CTA only ever waits on tiles that
 // are already resident; every wait is additionally bounded, and a wait that
 // runs out sets a device error bit instead of spinning on.
+#include <mutex>
+
 #include "pbf_device.cuh"
 
 namespace pbf {
@@ -30,7 +34,7 @@ constexpr uint32_t kLbAggregate = 1u << 30;
 constexpr uint32_t kLbInclusive = 2u << 30;
 constexpr uint32_t kSpinLimit = 1u << 22;
 constexpr int kSortWarps = kSortThreads / 32;
-static_assert(kSortThreads == kRadix, "one thread per digit in the scan");
+static_assert(kSortThreads == (1 << kMinDigitBits), "at least one digit per scan thread");
 
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) {
   return *reinterpret_cast<const volatile uint32_t *>(p);
@@ -67,29 +71,44 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v,
 
 __global__ void __launch_bounds__(256)
     k_sort_histogram(const uint32_t *__restrict__ keys, uint32_t n,
-                     uint32_t passes, uint32_t *__restrict__ hist) {
-  __shared__ uint32_t s_hist[kMaxSortPasses * kRadix];
-  for (uint32_t i = threadIdx.x; i < passes * kRadix; i += blockDim.x) s_hist[i] = 0;
+                     uint32_t passes, uint32_t digit_bits, uint32_t *__restrict__ hist) {
+  __shared__ uint32_t s_hist[kMaxHistWords];
+  const uint32_t hist_words = passes << digit_bits;
+  for (uint32_t i = threadIdx.x; i < hist_words; i += blockDim.x) s_hist[i] = 0;
   __syncthreads();
   const uint32_t stride = gridDim.x * blockDim.x;
   // Whole warps iterate together so that __match_any_sync sees every lane.
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
     const uint32_t i = base + threadIdx.x;
     const bool valid = i < n;
-    warp_digit_histogram(valid ? keys[i] : 0u, valid, passes, s_hist);
+    warp_digit_histogram(valid ? keys[i] : 0u, valid, passes, digit_bits, s_hist);
   }
   __syncthreads();
-  for (uint32_t i = threadIdx.x; i < passes * kRadix; i += blockDim.x)
+  for (uint32_t i = threadIdx.x; i < hist_words; i += blockDim.x)
     if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
 }
 
+// Exclusive prefix of each pass histogram, in place: each thread owns
+// radix / 256 consecutive digits.
 __global__ void __launch_bounds__(kSortThreads)
-    k_sort_scan(uint32_t passes, uint32_t *__restrict__ hist) {
+    k_sort_scan(uint32_t passes, uint32_t digit_bits, uint32_t *__restrict__ hist) {
   __shared__ uint32_t s_warp[kSortWarps];
+  constexpr uint32_t kMaxPer = 1u << (kMaxDigitBits - kMinDigitBits);
+  const uint32_t per = 1u << (digit_bits - kMinDigitBits);
   for (uint32_t p = 0; p < passes; ++p) {
-    const uint32_t v = hist[p * kRadix + threadIdx.x];
-    const uint32_t e = block_exclusive_scan(v, s_warp);
-    hist[p * kRadix + threadIdx.x] = e;
+    uint32_t *h = hist + (p << digit_bits) + threadIdx.x * per;
+    uint32_t v[kMaxPer], sum = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < kMaxPer; ++j) {
+      v[j] = j < per ? h[j] : 0u;
+      sum += v[j];
+    }
+    uint32_t e = block_exclusive_scan(sum, s_warp);
+#pragma unroll
+    for (uint32_t j = 0; j < kMaxPer; ++j) {
+      if (j < per) h[j] = e;
+      e += v[j];
+    }
     __syncthreads();
   }
 }
@@ -98,13 +117,14 @@ __global__ void __launch_bounds__(kSortThreads)
 // words, waiting for predecessors that have not published yet.  A wait of
 // more than spin_limit polls sets kDevErrLookback in *err and gives up
 // (returning what it has), so a kernel never spins without bound.
-__device__ __forceinline__ uint32_t lookback_prefix(uint32_t *lookback, uint32_t tile, uint32_t d,
+__device__ __forceinline__ uint32_t lookback_prefix(uint32_t *lookback, uint32_t radix,
+                                                    uint32_t tile, uint32_t d,
                                                     uint32_t spin_limit, uint32_t *err) {
   uint32_t excl = 0;
   int t = (int)tile - 1;
   uint32_t spins = 0;
   while (true) {
-    const uint32_t v = ld_volatile(&lookback[(size_t)t * kRadix + d]);
+    const uint32_t v = ld_volatile(&lookback[(size_t)t * radix + d]);
     const uint32_t flag = v & ~kLbMask;
     if (flag == 0u) {
       if (++spins >= spin_limit) {
@@ -125,10 +145,16 @@ __device__ __forceinline__ uint32_t lookback_prefix(uint32_t *lookback, uint32_t
 // never publishes (the words are zero): the wait must give up after
 // spin_limit polls and report through *err.
 __global__ void k_wait_selftest(uint32_t *lookback, uint32_t spin_limit, uint32_t *err) {
-  if (threadIdx.x == 0) lookback_prefix(lookback, 1u, 0u, spin_limit, err);
+  if (threadIdx.x == 0) lookback_prefix(lookback, 1u << kMinDigitBits, 1u, 0u, spin_limit, err);
 }
 
-template <bool kIota>
+// Dynamic shared memory of one digit pass with 2^kBits digits.
+constexpr size_t onesweep_smem_bytes(uint32_t bits) {
+  return ((size_t)kSortWarps * (1u << bits) + 2u * (1u << bits) + 2u * kSortTile) *
+         sizeof(uint32_t);
+}
+
+template <uint32_t kBits, bool kIota>
 __global__ void __launch_bounds__(kSortThreads)
     k_onesweep(const uint32_t *__restrict__ keys_in,
                const uint32_t *__restrict__ vals_in,
@@ -136,18 +162,20 @@ __global__ void __launch_bounds__(kSortThreads)
                uint32_t n, uint32_t shift,
                const uint32_t *__restrict__ global_excl,
                uint32_t *lookback, uint32_t *tile_counter, uint32_t *err) {
+  constexpr uint32_t R = 1u << kBits;
+  constexpr uint32_t kDig = R / kSortThreads;  // digits per thread, per-digit phases
+  extern __shared__ __align__(16) uint32_t s_dyn[];
+  uint32_t(*s_wcnt)[R] = reinterpret_cast<uint32_t(*)[R]>(s_dyn);  // [kSortWarps][R]
+  uint32_t *s_dexcl = s_dyn + kSortWarps * R;
+  uint32_t *s_gbase = s_dexcl + R;
+  uint32_t *s_keys = s_gbase + R;
+  uint32_t *s_vals = s_keys + kSortTile;
   __shared__ uint32_t s_tile;
-  __shared__ uint32_t s_wcnt[kSortWarps][kRadix];
-  __shared__ uint32_t s_dexcl[kRadix];
-  __shared__ uint32_t s_gbase[kRadix];
   __shared__ uint32_t s_warp[kSortWarps];
-  __shared__ uint32_t s_keys[kSortTile];
-  __shared__ uint32_t s_vals[kSortTile];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) s_tile = atomicAdd(tile_counter, 1u);
-  for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads)
-    (&s_wcnt[0][0])[i] = 0u;
+  for (uint32_t i = tid; i < kSortWarps * R; i += kSortThreads) (&s_wcnt[0][0])[i] = 0u;
   __syncthreads();
 
   const uint32_t tile = s_tile;
@@ -172,7 +200,7 @@ __global__ void __launch_bounds__(kSortThreads)
   for (int it = 0; it < kSortItems; ++it) {
     const uint32_t idx = seg + (uint32_t)it * 32u + lane;
     const bool ok = idx < n;
-    const uint32_t d = (key[it] >> shift) & (kRadix - 1);
+    const uint32_t d = (key[it] >> shift) & (R - 1);
     const unsigned peers = __match_any_sync(0xffffffffu, ok ? d : 0xffffffffu);
     const uint32_t before = ok ? s_wcnt[warp][d] : 0u;
     __syncwarp();
@@ -183,28 +211,48 @@ __global__ void __launch_bounds__(kSortThreads)
   }
   __syncthreads();
 
-  // Per digit: the tile's count, and each warp's exclusive offset.
-  const uint32_t d = (uint32_t)tid;
-  uint32_t tile_count = 0;
+  // Per digit (kDig consecutive digits per thread): the tile's count, and
+  // each warp's exclusive offset.
+  uint32_t tile_count[kDig], excl[kDig];
+  uint32_t sum = 0;
 #pragma unroll
-  for (int w = 0; w < kSortWarps; ++w) {
-    const uint32_t c = s_wcnt[w][d];
-    s_wcnt[w][d] = tile_count;
-    tile_count += c;
+  for (uint32_t j = 0; j < kDig; ++j) {
+    const uint32_t d = (uint32_t)tid * kDig + j;
+    uint32_t c = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) {
+      const uint32_t x = s_wcnt[w][d];
+      s_wcnt[w][d] = c;
+      c += x;
+    }
+    tile_count[j] = c;
+    excl[j] = 0;
+    sum += c;
   }
 
-  // Decoupled look-back for this digit.
-  uint32_t excl = 0;
+  // Decoupled look-back: publish every aggregate before waiting on any.
   if (tile == 0) {
-    st_volatile(&lookback[d], kLbInclusive | tile_count);
+#pragma unroll
+    for (uint32_t j = 0; j < kDig; ++j)
+      st_volatile(&lookback[(uint32_t)tid * kDig + j], kLbInclusive | tile_count[j]);
   } else {
-    st_volatile(&lookback[(size_t)tile * kRadix + d], kLbAggregate | tile_count);
-    excl = lookback_prefix(lookback, tile, d, kSpinLimit, err);
-    st_volatile(&lookback[(size_t)tile * kRadix + d],
-                kLbInclusive | ((excl + tile_count) & kLbMask));
+    uint32_t *mine = lookback + (size_t)tile * R + (uint32_t)tid * kDig;
+#pragma unroll
+    for (uint32_t j = 0; j < kDig; ++j) st_volatile(&mine[j], kLbAggregate | tile_count[j]);
+#pragma unroll
+    for (uint32_t j = 0; j < kDig; ++j) {
+      excl[j] = lookback_prefix(lookback, R, tile, (uint32_t)tid * kDig + j, kSpinLimit, err);
+      st_volatile(&mine[j], kLbInclusive | ((excl[j] + tile_count[j]) & kLbMask));
+    }
   }
-  s_gbase[d] = global_excl[d] + excl;
-  s_dexcl[d] = block_exclusive_scan(tile_count, s_warp);
+  uint32_t e = block_exclusive_scan(sum, s_warp);
+#pragma unroll
+  for (uint32_t j = 0; j < kDig; ++j) {
+    const uint32_t d = (uint32_t)tid * kDig + j;
+    s_gbase[d] = global_excl[d] + excl[j];
+    s_dexcl[d] = e;
+    e += tile_count[j];
+  }
   __syncthreads();
 
   // Stage the tile in digit order in shared memory, then write it out with
@@ -213,7 +261,7 @@ __global__ void __launch_bounds__(kSortThreads)
   for (int it = 0; it < kSortItems; ++it) {
     const uint32_t idx = seg + (uint32_t)it * 32u + lane;
     if (idx < n) {
-      const uint32_t dg = (key[it] >> shift) & (kRadix - 1);
+      const uint32_t dg = (key[it] >> shift) & (R - 1);
       const uint32_t lp = s_dexcl[dg] + s_wcnt[warp][dg] + rank[it];
       s_keys[lp] = key[it];
       s_vals[lp] = val[it];
@@ -223,7 +271,7 @@ __global__ void __launch_bounds__(kSortThreads)
   const uint32_t tile_n = min((uint32_t)kSortTile, n - tile_base);
   for (uint32_t i = tid; i < tile_n; i += kSortThreads) {
     const uint32_t k = s_keys[i];
-    const uint32_t dg = (k >> shift) & (kRadix - 1);
+    const uint32_t dg = (k >> shift) & (R - 1);
     const uint32_t dst = s_gbase[dg] + (i - s_dexcl[dg]);
     // Always true unless a look-back wait gave up (error flag set).
     if (dst < n) {
@@ -231,6 +279,45 @@ __global__ void __launch_bounds__(kSortThreads)
       vals_out[dst] = s_vals[i];
     }
   }
+}
+
+// Every instantiation takes its tile's shared memory dynamically (above the
+// 48 KB static limit with 9-bit digits); the limit is raised once.
+std::once_flag g_onesweep_once;
+cudaError_t g_onesweep_status = cudaSuccess;
+
+template <uint32_t kBits>
+cudaError_t allow_onesweep_smem() {
+  const int bytes = (int)onesweep_smem_bytes(kBits);
+  cudaError_t e = cudaFuncSetAttribute(k_onesweep<kBits, false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_onesweep<kBits, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  return e;
+}
+
+cudaError_t onesweep_init() {
+  std::call_once(g_onesweep_once, [] {
+    cudaError_t e = allow_onesweep_smem<8>();
+    if (e == cudaSuccess) e = allow_onesweep_smem<9>();
+    g_onesweep_status = e;
+  });
+  return g_onesweep_status;
+}
+
+template <uint32_t kBits>
+void launch_onesweep(bool iota, uint32_t tiles, cudaStream_t stream, const uint32_t *ksrc,
+                     const uint32_t *vsrc, uint32_t *kdst, uint32_t *vdst, uint32_t n,
+                     uint32_t shift, const uint32_t *hist, uint32_t *lb, uint32_t *ctr,
+                     uint32_t *err) {
+  const size_t smem = onesweep_smem_bytes(kBits);
+  if (iota)
+    k_onesweep<kBits, true><<<tiles, kSortThreads, smem, stream>>>(ksrc, nullptr, kdst, vdst, n,
+                                                                  shift, hist, lb, ctr, err);
+  else
+    k_onesweep<kBits, false><<<tiles, kSortThreads, smem, stream>>>(ksrc, vsrc, kdst, vdst, n,
+                                                                   shift, hist, lb, ctr, err);
 }
 
 // off[c] = number of sorted keys < c, for c in [0, ncells]: one thread per
@@ -320,30 +407,6 @@ uint32_t bits_for(uint32_t max_key_exclusive) {
   return b;
 }
 
-SortPlan make_sort_plan(uint32_t n, uint32_t key_bits) {
-  SortPlan p;
-  p.n = n;
-  p.key_bits = key_bits < 1 ? 1 : (key_bits > 32 ? 32 : key_bits);
-  p.passes = (p.key_bits + kRadixBits - 1) / kRadixBits;
-  p.tiles = (uint32_t)(((uint64_t)n + kSortTile - 1) / kSortTile);
-  size_t w = 0;
-  p.off_hist = w;
-  w += (size_t)p.passes * kRadix;
-  p.off_counter = w;
-  w += 32;
-  p.off_lookback = w;
-  w += (size_t)p.passes * p.tiles * kRadix;
-  p.clear_words = w - p.off_hist;
-  w = (w + 63) & ~size_t(63);
-  p.off_keys_alt = w;
-  w += (size_t)n;
-  w = (w + 63) & ~size_t(63);
-  p.off_vals_alt = w;
-  w += (size_t)n;
-  p.words = w;
-  return p;
-}
-
 uint32_t sort_pass_launches(const SortPlan &plan) { return 2u + plan.passes; }
 
 cudaError_t wait_selftest(uint32_t *scratch, uint32_t spin_limit, uint32_t *err,
@@ -362,14 +425,14 @@ cudaError_t sort_histogram(const SortPlan &plan, const uint32_t *keys,
                            uint32_t *scratch, cudaStream_t stream) {
   if (plan.n == 0) return cudaSuccess;
   const uint32_t blocks = min(blocks_for(plan.n, 256), kStrideCtas);
-  k_sort_histogram<<<blocks, 256, 0, stream>>>(keys, plan.n, plan.passes,
+  k_sort_histogram<<<blocks, 256, 0, stream>>>(keys, plan.n, plan.passes, plan.digit_bits,
                                                scratch + plan.off_hist);
   return cudaGetLastError();
 }
 
 cudaError_t sort_scan(const SortPlan &plan, uint32_t *scratch,
                       cudaStream_t stream) {
-  k_sort_scan<<<1, kSortThreads, 0, stream>>>(plan.passes,
+  k_sort_scan<<<1, kSortThreads, 0, stream>>>(plan.passes, plan.digit_bits,
                                               scratch + plan.off_hist);
   return cudaGetLastError();
 }
@@ -379,6 +442,11 @@ cudaError_t sort_passes(const SortPlan &plan, const uint32_t *keys_in,
                         uint32_t *vals_out, uint32_t *scratch, uint32_t *err,
                         cudaStream_t stream) {
   if (plan.n == 0) return cudaSuccess;
+  if (plan.digit_bits < kMinDigitBits || plan.digit_bits > kMaxDigitBits ||
+      plan.passes > (uint32_t)kMaxSortPasses)
+    return cudaErrorInvalidValue;
+  const cudaError_t init = onesweep_init();
+  if (init != cudaSuccess) return init;
   uint32_t *kalt = scratch + plan.off_keys_alt;
   uint32_t *valt = scratch + plan.off_vals_alt;
   // Arrange the ping-pong so the last pass writes keys_out/vals_out and the
@@ -389,16 +457,17 @@ cudaError_t sort_passes(const SortPlan &plan, const uint32_t *keys_in,
     const bool to_out = ((plan.passes - 1 - p) % 2) == 0;
     uint32_t *kdst = to_out ? keys_out : kalt;
     uint32_t *vdst = to_out ? vals_out : valt;
-    uint32_t *hist = scratch + plan.off_hist + (size_t)p * kRadix;
-    uint32_t *lb = scratch + plan.off_lookback + (size_t)p * plan.tiles * kRadix;
+    uint32_t *hist = scratch + plan.off_hist + (size_t)p * plan.radix;
+    uint32_t *lb = scratch + plan.off_lookback + (size_t)p * plan.tiles * plan.radix;
     uint32_t *ctr = scratch + plan.off_counter + p;
-    if (p == 0 && vsrc == nullptr) {
-      k_onesweep<true><<<plan.tiles, kSortThreads, 0, stream>>>(
-          ksrc, nullptr, kdst, vdst, plan.n, p * kRadixBits, hist, lb, ctr, err);
-    } else {
-      k_onesweep<false><<<plan.tiles, kSortThreads, 0, stream>>>(
-          ksrc, vsrc, kdst, vdst, plan.n, p * kRadixBits, hist, lb, ctr, err);
-    }
+    const bool iota = p == 0 && vsrc == nullptr;
+    const uint32_t shift = p * plan.digit_bits;
+    if (plan.digit_bits == 8)
+      launch_onesweep<8>(iota, plan.tiles, stream, ksrc, vsrc, kdst, vdst, plan.n, shift, hist,
+                         lb, ctr, err);
+    else
+      launch_onesweep<9>(iota, plan.tiles, stream, ksrc, vsrc, kdst, vdst, plan.n, shift, hist,
+                         lb, ctr, err);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     ksrc = kdst;

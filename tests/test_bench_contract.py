@@ -29,7 +29,17 @@ def test_traffic_lines_for_every_timed_kernel():
 def test_algorithmic_bytes_sum_to_the_step_total():
     per_step = {"predict_hash": 1, "sort_onesweep": 1, "cell_offsets": 1, "reorder": 1,
                 "lambda": 4, "delta": 4, "vorticity": 1, "xsph_commit": 1}
-    assert sum(bench.ALG_BYTES[k] * m for k, m in per_step.items()) == bench.STEP_BYTES
+    cells_64 = 64 ** 3
+    assert sum(bench.ALG_BYTES[k] * m for k, m in per_step.items()) == bench.step_bytes(cells_64)
+    assert bench.sort_bytes(cells_64) == bench.ALG_BYTES["sort_onesweep"] == 4 + 16 * 2
+
+
+def test_sort_passes_follow_the_digit_plan():
+    # 9-bit digits only for 9 and 17-18 key bits; 8-bit digits otherwise
+    want = {1: 1, 8: 1, 9: 1, 10: 2, 16: 2, 17: 2, 18: 2, 19: 3, 20: 3, 24: 3, 25: 4,
+            27: 4, 32: 4}
+    assert {b: bench.sort_passes(b) for b in want} == want
+    assert bench.sort_key_bits(128 * 128 * 64) == 20 and bench.sort_bytes(128 * 128 * 64) == 52
 
 
 def test_measured_peaks_has_a_bandwidth():

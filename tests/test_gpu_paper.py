@@ -154,14 +154,28 @@ def test_checkpoint_resume(pbf, tmp_path):
 
 
 def test_stage_timing_reports_four_stages(pbf):
+    """Stage-timed steps (each captured with its boundary events and launched
+    as one graph) report every stage and kernel and give the bits of untimed
+    steps."""
     sc = pbf.scenes.dam_break((12, 12, 12), (0.8, 0.8, 0.8), seed=9)
     with pbf.Simulation(sc.params, sc.particles) as sim:
         sim.init()
         sim.set_stage_timing(True)
-        sim.step(2)
+        sim.step(3)
         ms = sim.stage_times()
+        kt = sim.kernel_times()
+        timed = sim.dumpData()
         assert (ms > 0).all() and np.isfinite(ms).all()
         assert sim.launches_per_step() >= 10
+        assert {"predict_hash", "sort_onesweep", "reorder", "delta", "xsph_commit"} <= set(kt)
+        assert all(t > 0 for t, _ in kt.values())
+    with pbf.Simulation(sc.params, sc.particles) as sim:
+        sim.init()
+        sim.step(3)
+        plain = sim.dumpData()
+    for a, b in zip(timed, plain):
+        assert np.array_equal(np.ascontiguousarray(a).view(np.uint32),
+                              np.ascontiguousarray(b).view(np.uint32))
 
 
 def test_cells_are_a_valid_neighbour_structure(pbf):

@@ -47,6 +47,16 @@ CASES = [
     ("bits24", 200_000, 24, "uniform"),
     ("bits32", 200_000, 32, "uniform"),
     ("clustered", 1 << 20, 18, "clustered"),
+    # the plans around the 9-bit ones (9 and 17-18 bits): two 8-bit passes
+    # (10), two 9-bit (17), three 8-bit (19, 20), four 8-bit (27-31)
+    ("bits10", 50_000, 10, "uniform"),
+    ("bits17", 200_000, 17, "uniform"),
+    ("bits19", 200_000, 19, "uniform"),
+    ("bits20_tile_plus", 4097, 20, "uniform"),
+    ("bits27", 200_000, 27, "uniform"),
+    ("bits30", 200_000, 30, "uniform"),
+    ("bits31", 200_000, 31, "uniform"),
+    ("clustered20", 1 << 20, 20, "clustered"),
 ]
 
 
@@ -75,6 +85,18 @@ def test_sort_pairs_is_the_stable_permutation(pbf, name, n, bits, kind):
     want = np.argsort(keys, kind="stable").astype(np.uint32)
     assert np.array_equal(perm, want)
     assert np.array_equal(sk, keys[want])
+
+
+def test_digit_widths_give_the_same_permutation(pbf):
+    """18-bit keys sorted as 18 bits (two 9-bit passes), 20 and 24 bits
+    (three 8-bit passes), 30 and 32 bits (four 8-bit passes): one stable
+    permutation."""
+    rng = np.random.default_rng(7)
+    keys = make_keys("clustered", 500_000, 18, rng)
+    first = gpu_sort(pbf, keys, 18)
+    for bits in (20, 24, 30, 32):
+        got = gpu_sort(pbf, keys, bits)
+        assert np.array_equal(got[0], first[0]) and np.array_equal(got[1], first[1]), bits
 
 
 def test_sort_pairs_carries_values(pbf):
