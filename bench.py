@@ -420,30 +420,39 @@ def ref_equations_run(pbf, sc, args) -> dict:
                       "host buffers, the state up and down every step"}
 
 
-def fp64_step_error(pbf, sim, params) -> dict:
-    """One more step of the simulation from its current state against the
-    FP64 oracle of the same equations from the same state (outside every
-    timed region): largest position and velocity difference, in h and m/s."""
+def fp64_step_error(pbf, sim, params, state=None, where: str = "the state after the timed steps") -> dict:
+    """One step of the simulation from `state` (default: its current state)
+    against the FP64 oracle of the same equations from the same state
+    (outside every timed region): largest position and velocity difference,
+    in h and m/s, and how the position differences are distributed."""
     import oracle
     import __graft_entry__ as ge
 
-    pos, vel = sim.dumpData()
+    pos, vel = state if state is not None else sim.dumpData()
     sim.set_state(pos, vel)
     sim.step(1)
     gpos, gvel = sim.dumpData()
     t0 = time.perf_counter()
-    opos, ovel, *_ = oracle.paper_steps_f64(ge.paper_params_for_oracle(params), pos, vel, 1)
+    prm = ge.paper_params_for_oracle(params)
+    opos, ovel, *_ = oracle.paper_steps_f64(prm, pos, vel, 1)
     ex = np.abs(gpos[:, :3].astype(np.float64) - opos[:, :3]).max(axis=1) / params.h
     dv = np.abs(gvel[:, :3].astype(np.float64) - ovel[:, :3]).max()
+    # the same step evaluated in binary32 on the host (IEEE operations, the
+    # oracle's own order): how far binary32 itself lands from FP64 here
+    cpos, *_ = oracle.paper_steps_f64(prm, pos, vel, 1, precision="f32")
+    cx = np.abs(cpos[:, :3] - opos[:, :3]).max(axis=1) / params.h
     # particles stacked on one point (clamped into a corner of the box) do
     # not interact (r = 0) and can carry speeds where one step is chaotic
     stacked = int(pos.shape[0] - np.unique(pos[:, :3], axis=0).shape[0])
     return {"position_max_h": float(ex.max()), "position_p999_h": float(np.percentile(ex, 99.9)),
             "particles_over_bound": int((ex > 1e-5).sum()), "velocity_max": float(dv),
             "bound_position_h": 1e-5, "within_bound": bool(ex.max() <= 1e-5),
+            "host_binary32": {"position_max_h": float(cx.max()),
+                              "position_p999_h": float(np.percentile(cx, 99.9)),
+                              "particles_over_bound": int((cx > 1e-5).sum())},
             "stacked_particles": stacked, "oracle_s": time.perf_counter() - t0,
-            "method": "one step from the state after the timed steps, GPU (binary32) against "
-                      "the FP64 oracle restatement of the same equations from the same state"}
+            "method": f"one step from {where}, GPU (binary32) against the FP64 oracle "
+                      "restatement of the same equations from the same state"}
 
 
 def run_ours(args) -> int:
@@ -492,7 +501,7 @@ def run_ours(args) -> int:
     density_error = density_error_of(sim, sc.params.rest_density, args.warmup + args.steps)
     nbr_max, nbr_over = sim.neighbour_stats()
     tiles = sim.tile_stats()
-    fp64_err = fp64_step_error(pbf, sim, sc.params) if rank == 0 and not args.no_fp64 else None
+    fp64_end = fp64_step_error(pbf, sim, sc.params) if rank == 0 and not args.no_fp64 else None
 
     # ---- end to end through the C-ABI with host buffers ------------------
     nbytes = n * 16
@@ -534,6 +543,11 @@ def run_ours(args) -> int:
     kt = sim.kernel_times()
     stages = sim.stage_times()
     sim.set_stage_timing(False)
+    fp64_err = None
+    if fp64_end is not None:
+        fp64_err = {"at_start": fp64_step_error(pbf, sim, sc.params, start_state,
+                                                f"the timed steps' start state (step {args.warmup})"),
+                    "at_end": fp64_end}
     total_ms = sum(ms for ms, _ in kt.values())
     dom = max((k for k in kt if k in ALG_BYTES), key=lambda k: kt[k][0])
     dom_ms, dom_launches = kt[dom]
