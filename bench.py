@@ -24,9 +24,11 @@ Our arm prints one JSON line with:
             back after the timed region;
   neighbour_lists  the final step's largest neighbour count and how many
             particles exceeded the list capacity (and re-derived their sets);
-  fp64_step_error  one more step from the final state against the FP64
-            oracle of the same equations from the same state (largest
-            position difference in h; the bound is 1e-5 h), untimed;
+  fp64_step_error  one step from the timed steps' start state and one from
+            their final state against the FP64 oracle of the same equations
+            from the same state (largest position difference in h, its
+            distribution; the bound is 1e-5 h), beside the same step in
+            binary32 on the host, untimed;
   equations "paper": the line's value runs Macklin & Mueller's equations;
   ref_equations  the same scene in REF_COMPAT mode (the reference kernels'
             own equations, bit-exact with them): device-resident and end to
@@ -46,6 +48,12 @@ larger than L2, so no flush runs between steps.
             scene latency.
 Before warm-up each workload runs the launch-shape tuner on its own scenes
 (--no-tune keeps the defaults; results are bitwise the same either way).
+
+--workload small: the 32,768-particle dam break (32^3 block in a 1.6 x 1.6
+x 3.2 box), 500 steps; its reference arm runs the paper equations of that
+configuration on the host cores for all 500 steps (the oracle's binary32
+restatement: the reference's kernels have no s_corr or vorticity) beside
+the reference's own kernels for their first 20 steps.
 
 --workload batch: 256 independent dam breaks, N log-uniform 4,096..262,144,
 block aspect ratios in [0.5, 2], boxes twice the block extent, advanced
@@ -300,7 +308,8 @@ def cpu_reference_run(n_steps_max: int = 50, budget_s: float = 15.0, threads: in
     this leg loads nothing of the product library.  Returns (value, info)."""
     import oracle
 
-    cfg, pos, vel = oracle.scene_4m() if workload == "large" else oracle.scene_1m()
+    cfg, pos, vel = {"large": oracle.scene_4m, "small": oracle.scene_small}.get(
+        workload, oracle.scene_1m)()
     n = pos.shape[0]
     threads = threads or (os.cpu_count() or 1)
     kind = "reference" if oracle.reference_available() else "port"
@@ -324,11 +333,41 @@ def cpu_reference_run(n_steps_max: int = 50, budget_s: float = 15.0, threads: in
     return value, info
 
 
+def cpu_paper_run(steps: int, threads: int = 0, workload: str = "small", chunk: int = 25):
+    """The paper equations of the benchmark configuration on the host cores:
+    the oracle's binary32 restatement (the reference's kernels have no
+    s_corr or vorticity), `steps` steps from the scene's initial state in
+    chunks of `chunk`.  Returns (value, info)."""
+    import oracle
+
+    cfg, pos, vel = {"large": oracle.scene_4m, "single": oracle.scene_1m}.get(
+        workload, oracle.scene_small)()
+    prm = oracle.benchmark_paper_params(cfg)
+    n = pos.shape[0]
+    threads = threads or (os.cpu_count() or 1)
+    done = 0
+    t0 = time.perf_counter()
+    while done < steps:
+        k = min(chunk, steps - done)
+        pos, vel, *_ = oracle.paper_steps_f64(prm, pos, vel, k, threads=threads, precision="f32")
+        done += k
+    dt = time.perf_counter() - t0
+    value = n * ITERATIONS * done / dt
+    finite = bool(np.isfinite(pos).all())
+    info = {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "equations": "paper",
+            "steps": done, "finite": finite,
+            "sample": f"all {done} steps of the {n}-particle scene from its initial state, paper "
+                      f"equations, the oracle's binary32 restatement on {threads} threads, {dt:.1f} s"}
+    return value, info
+
+
 # -------------------------------------------------------------------- arms
 def run_reference(args) -> int:
     world, rank, _ = dist_info()
     if rank != 0:
         return 0
+    if args.workload == "small":
+        return run_reference_small(args)
     value, info = cpu_reference_run(n_steps_max=max(1, args.steps), budget_s=args.cpu_budget,
                                     workload=args.workload)
     large = args.workload == "large"
@@ -343,6 +382,29 @@ def run_reference(args) -> int:
                    "equations": "reference kernels (relaxation 1e4, no s_corr, XSPH, no vorticity)",
                    "note": "the like-for-like GPU figure is the headline line's ref_equations"},
         "cpu_baseline": info,
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_reference_small(args) -> int:
+    """The 32,768-particle configuration on the host cores: all its steps in
+    the paper equations it names (the oracle's binary32 restatement), and
+    the reference's own kernels on the same scene for their first 20 steps
+    (its equations push this block out of its box after ~30 steps)."""
+    value, info = cpu_paper_run(max(1, args.steps), workload="small")
+    _, kernels = cpu_reference_run(n_steps_max=20, budget_s=args.cpu_budget, workload="small")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": info["steps"], "warmup": 0, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "equations": "paper",
+        "config": {"workload": "dam_break_32k", "particles": 32768, "cells": 16 * 16 * 32,
+                   "box": [1.6, 1.6, 3.2], "solver_iterations": ITERATIONS,
+                   "equations": "paper (relaxation 600, s_corr, XSPH, vorticity)"},
+        "cpu_baseline": info,
+        "reference_kernels": kernels,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -464,7 +526,8 @@ def run_ours(args) -> int:
     torch.cuda.set_device(local)
     dist = make_group(world, "nccl")
     pbf = ge.load_package()
-    sc = pbf.scenes.config_4m() if args.workload == "large" else pbf.scenes.config_1m()
+    sc = {"large": pbf.scenes.config_4m, "small": pbf.scenes.config_small}.get(
+        args.workload, pbf.scenes.config_1m)()
     if args.max_neighbours:
         sc.params.max_neighbours = args.max_neighbours
     n = sc.n
@@ -573,7 +636,10 @@ def run_ours(args) -> int:
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        _, cpu = cpu_reference_run(budget_s=args.cpu_budget, workload=args.workload)
+        if args.workload == "small":
+            _, cpu = cpu_paper_run(min(args.steps, 500), workload="small")
+        else:
+            _, cpu = cpu_reference_run(budget_s=args.cpu_budget, workload=args.workload)
 
     sim.close()
     ref_eq = ref_equations_run(pbf, sc, args) if world == 1 else None
@@ -983,11 +1049,11 @@ def main() -> int:
                     help="timed steps (default 500 for the single scene, 300 for the batch)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["single", "large", "batch", "serve", "aux"],
+    ap.add_argument("--workload", choices=["single", "small", "large", "batch", "serve", "aux"],
                     default="single",
-                    help="single: the 1M-particle scene (headline); large: the 4.2M-particle double "
-                         "dam break; batch; serve; aux: scenario I/O, runner snapshots and "
-                         "rendering around the 1M step")
+                    help="single: the 1M-particle scene (headline); small: the 32,768-particle "
+                         "dam break; large: the 4.2M-particle double dam break; batch; serve; "
+                         "aux: scenario I/O, runner snapshots and rendering around the 1M step")
     ap.add_argument("--serve-seconds", type=float, default=6.0, help="arrival window of the served stream")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="mean requests per second of the served stream")
     ap.add_argument("--steady-seconds", type=float, default=20.0,

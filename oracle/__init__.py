@@ -232,6 +232,38 @@ def dam_break_scene(dims, box, seed: int = 0x5EED):
     return cfg, pos, vel
 
 
+def scene_small(seed: int = 0x5EED):
+    """The 32,768-particle dam break (32^3 block in a 1.6 x 1.6 x 3.2 box,
+    16 x 16 x 32 cells)."""
+    return dam_break_scene((32, 32, 32), (1.6, 1.6, 3.2), seed)
+
+
+def benchmark_paper_params(cfg: "Config") -> PaperParams:
+    """The FP64 oracle's parameters of the benchmark's paper equations on
+    `cfg`'s box: h 0.1, 4 iterations, relaxation 600, s_corr k 0.1 n 4
+    dq 0.2 h, XSPH 0.01, vorticity 0.0005, gravity -9.81 along y, walls h/4
+    inside the box; each value rounded to binary32 first, as the library's
+    parameter block holds it."""
+    f = lambda v: float(np.float32(v))  # noqa: E731
+    o = PaperParams()
+    o.box_min[:] = [cfg.x_min, cfg.y_min, cfg.z_min]
+    o.box_max[:] = [cfg.x_max, cfg.y_max, cfg.z_max]
+    o.n_cells[:] = [int(cfg.x_n), int(cfg.y_n), int(cfg.z_n)]
+    o.iterations = 4
+    o.dt = cfg.timestep_length
+    o.rest_density = cfg.rest_density
+    o.h = f(0.1)
+    o.relax_eps = f(600.0)
+    o.scorr_k = f(0.1)
+    o.scorr_dq = f(0.2)
+    o.scorr_n = 4
+    o.xsph_c = f(0.01)
+    o.vort_eps = f(0.0005)
+    o.gravity_y = f(-9.81)
+    o.wall_margin = f(0.25 * f(0.1))
+    return o
+
+
 def scene_1m(seed: int = 0x5EED):
     """The 1,048,576-particle headline scene (128 x 128 x 64 block, 6.4 m
     cube, 64^3 cells)."""

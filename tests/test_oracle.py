@@ -258,13 +258,20 @@ def test_oracle_scenes_match_the_library_generator(oracle_mod):
         pos, vel = oracle_mod.generate_block((0.025, 0.025, 0.025), dims, 0.05, 0.0005, 0.125, seed)
         assert np.array_equal(bits(pos), bits(want_pos)), dims
         assert np.array_equal(bits(vel), bits(want_vel)), dims
-    cfg, pos, vel = oracle_mod.scene_1m()
-    sc = pbf.scenes.config_1m()
-    want_pos, want_vel = pbf.state_from_particles(sc.particles)
-    assert np.array_equal(bits(pos), bits(want_pos))
-    assert np.array_equal(bits(vel), bits(want_vel))
-    p = sc.params
-    for f, g in [("x_min", "x_min"), ("x_max", "x_max"), ("y_max", "y_max"), ("z_max", "z_max"),
-                 ("x_n", "x_n"), ("y_n", "y_n"), ("z_n", "z_n"),
-                 ("timestep_length", "time_step_length"), ("rest_density", "rest_density")]:
-        assert np.float32(getattr(cfg, f)) == np.float32(getattr(p, g)), f
+    for (cfg, pos, vel), sc in [(oracle_mod.scene_1m(), pbf.scenes.config_1m()),
+                                (oracle_mod.scene_small(), pbf.scenes.config_small())]:
+        want_pos, want_vel = pbf.state_from_particles(sc.particles)
+        assert np.array_equal(bits(pos), bits(want_pos)), sc.name
+        assert np.array_equal(bits(vel), bits(want_vel)), sc.name
+        p = sc.params
+        for f, g in [("x_min", "x_min"), ("x_max", "x_max"), ("y_max", "y_max"), ("z_max", "z_max"),
+                     ("x_n", "x_n"), ("y_n", "y_n"), ("z_n", "z_n"),
+                     ("timestep_length", "time_step_length"), ("rest_density", "rest_density")]:
+            assert np.float32(getattr(cfg, f)) == np.float32(getattr(p, g)), (sc.name, f)
+        # the CPU arm's paper parameters are the product's for the same scene
+        a = oracle_mod.benchmark_paper_params(cfg)
+        b = ge.paper_params_for_oracle(p)
+        for f, _ in oracle_mod.PaperParams._fields_:
+            if f != "pad_":
+                assert list(np.atleast_1d(getattr(a, f))) == list(np.atleast_1d(getattr(b, f))), \
+                    (sc.name, f)
