@@ -109,11 +109,11 @@ UNIT = "particle-iterations/s"
 # (20 + 24).  Every kernel the step launches has an entry, so the roofline
 # object names the kernel that takes the most time.
 ALG_BYTES = {
-    "predict_hash": 72, "sort_onesweep": 36, "cell_offsets": 8, "reorder": 104,
+    "predict_hash": 72, "sort_onesweep": 36, "cell_offsets": 8, "cell_sort": 22, "reorder": 104,
     "nbr_build": 20, "nbr_lambda": 44, "lambda": 24, "delta": 36, "vorticity": 48,
     "xsph_commit": 84,
 }
-STEP_BYTES_BUT_SORT = 556
+STEP_BYTES_BUT_SORT = 556  # with the radix sort's cell offsets (8), without the sort
 
 
 def sort_passes(key_bits: int) -> int:
@@ -131,7 +131,17 @@ def sort_bytes(cells: int) -> int:
     return 4 + 16 * sort_passes(sort_key_bits(cells))
 
 
-def step_bytes(cells: int) -> int:
+def cell_sort_bytes(particles: int, cells: int) -> int:
+    """The counting sort by cell (the default sort of the step): read the
+    keys and each particle's place in its cell (8; the place is written by
+    the predict kernel, 4), write the sorted keys and the permutation (8),
+    read the counts and write the offsets (8 per cell), rounded."""
+    return int(round(20 + 8 * cells / max(particles, 1)))
+
+
+def step_bytes(cells: int, particles: int = 0, counting: bool = False) -> int:
+    if counting:  # the counting sort writes the cell offsets itself
+        return STEP_BYTES_BUT_SORT - ALG_BYTES["cell_offsets"] + cell_sort_bytes(particles, cells)
     return STEP_BYTES_BUT_SORT + sort_bytes(cells)
 
 
@@ -618,7 +628,9 @@ def run_ours(args) -> int:
     if dom == "sort_onesweep":
         per_launch_s = dom_ms / 1e3 / kt_steps
     peaks = measured_peaks()
-    alg = dict(ALG_BYTES, sort_onesweep=sort_bytes(sc.params.ncells))
+    alg = dict(ALG_BYTES, sort_onesweep=sort_bytes(sc.params.ncells),
+               cell_sort=cell_sort_bytes(n, sc.params.ncells))
+    counting = "cell_sort" in kt
     achieved = alg[dom] * n / per_launch_s / 1e9
     traffic = profile_traffic(dom)
     roofline = {
@@ -629,7 +641,7 @@ def run_ours(args) -> int:
         "avg_launch_ms": per_launch_s * 1e3, "share_of_step": dom_ms / total_ms,
     }
     step_s = t_dev / args.steps
-    sb = step_bytes(sc.params.ncells)
+    sb = step_bytes(sc.params.ncells, n, counting)
     step_roofline = {"bytes_per_particle_step": sb,
                      "achieved_gbs": sb * n / step_s / 1e9,
                      "frac": sb * n / step_s / 1e9 / peaks["hbm_gbs"]}
@@ -764,7 +776,7 @@ def run_batch(args, emit: bool = True):
     t_wall = reduce_max(dist, t_wall, device="cuda")
     e2e_value = world * work_e2e / t_wall
     peaks = measured_peaks()
-    batch_step_bytes = step_bytes(cells_tot)
+    batch_step_bytes = step_bytes(cells_tot, n_tot, counting=not (tuning or {}).get("radix_sort", 0))
     step_gbs = batch_step_bytes * n_tot / (t_dev / steps) / 1e9
 
     # ---- the same scenes one by one on the plain path ---------------------

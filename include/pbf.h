@@ -226,18 +226,22 @@ int pbf_launches_per_step(const pbf_sim *sim, uint32_t *launches);
  * lambda, 3 delta-p, 4 vorticity, 5 XSPH + commit.  threads = 64, 128 or
  * 256 per CTA; batch = 4 or 8 neighbour loads in flight per thread (ignored
  * for 0 and 1); fuse_first = 1 runs 1 instead of 0 + 2 for the first solver
- * iteration.  staged = 1 runs every gather pass on staged tiles instead: a
- * CTA per 128 sorted slots copies its neighbourhood into shared memory with
- * bulk asynchronous copies and the passes read neighbours from there
- * (threads, batch and fuse_first then do not apply).  No shape changes a
- * result bit.  trial_ms is the tuner's best time per launch of each pass (0
- * when untuned). */
+ * iteration.  staged = 1 runs every gather pass on staged cell blocks
+ * instead: persistent CTAs walk the step's occupied blocks of 4 x 4 x 4
+ * cells, copy each block's neighbourhood into shared memory with bulk
+ * asynchronous copies and read neighbours from there (threads, batch and
+ * fuse_first then do not apply).  radix_sort = 1 sorts the step's cell keys
+ * with the onesweep radix sort instead of the counting sort by cell (the
+ * default); both give the stable permutation.  No choice changes a result
+ * bit.  trial_ms is the tuner's best time per launch of each pass (0 when
+ * untuned). */
 typedef struct pbf_tuning {
   uint32_t threads[6];
   uint32_t batch[6];
   uint32_t fuse_first;
   float trial_ms[6];
   uint32_t staged;
+  uint32_t radix_sort;
 } pbf_tuning;
 /* Times every shape over `trial_steps` steps (1..32) of this simulation
  * from its current state, keeps the fastest per pass and restores the state
@@ -269,12 +273,12 @@ int pbf_neighbour_stats(pbf_sim *sim, uint32_t *max_count, uint32_t *overflow);
  * count right after that step -- while the step before still runs.)  No
  * reference counterpart; grows may be NULL. */
 int pbf_list_capacity(const pbf_sim *sim, uint32_t *capacity, uint32_t *grows);
-/* Staged tiles of the last step (PAPER mode with staged = 1 in the
- * tuning): how many 128-slot tiles staged their neighbourhood in shared
- * memory and how many gathered through L1 instead (more than three grid
- * rows in the tile, or more than 2048 candidates).  Both 0 when the last
- * step ran the L1 passes.  PBF_ERR_STATE in REF_COMPAT mode or before the
- * first step.  No reference counterpart. */
+/* Staged cell blocks of the last step (PAPER mode with staged = 1 in the
+ * tuning): how many occupied blocks of 4 x 4 x 4 cells staged their
+ * neighbourhood in shared memory and how many gathered through L1 instead
+ * (more than 3072 candidates in the block's neighbourhood).  Both 0 when
+ * the last step ran the L1 passes.  PBF_ERR_STATE in REF_COMPAT mode or
+ * before the first step.  No reference counterpart. */
 int pbf_tile_stats(pbf_sim *sim, uint32_t *staged, uint32_t *unstaged);
 /* The neighbour structure the last step built, in input particle order:
  * hash[i] = cell of particle i; perm[q] = input index of the particle at
@@ -457,6 +461,26 @@ int pbf_op_sort_pairs_noalloc(const uint32_t *d_keys_in,
                               uint32_t key_bits, uint32_t *d_keys_out,
                               uint32_t *d_vals_out, uint32_t *d_status,
                               void *stream);
+/* Bytes of device scratch pbf_op_sort_cells needs. */
+size_t pbf_op_sort_cells_scratch_bytes(uint32_t n, uint32_t ncells);
+/* The stable sort of cell keys (every key < ncells) in one counting pass,
+ * as the PAPER step sorts: d_offsets[c] = number of keys < c for c in
+ * [0, ncells] (the CSR cell offsets), d_sorted_keys and d_perm the stable
+ * order (ties by index: d_perm[q] = index of the q-th key), the same as
+ * pbf_op_sort_pairs with values NULL followed by pbf_op_cell_offsets.
+ * Keys are counted per cell with warp-aggregated atomics, the counts
+ * scanned into the offsets (decoupled look-back), every key scattered to its
+ * cell, and each cell put back in index order (in registers up to 16 keys,
+ * in shared memory up to 8192, through a bitmap of the indices beyond).
+ * Outputs must not alias the keys.  No reference counterpart beyond the
+ * intent of init_cells.cl + find_cells.cl + the radix kernels. */
+int pbf_op_sort_cells(const uint32_t *d_keys, uint32_t n, uint32_t ncells,
+                      uint32_t *d_offsets, uint32_t *d_sorted_keys, uint32_t *d_perm,
+                      void *d_scratch, size_t scratch_bytes, void *stream);
+/* Synchronises `stream` and reports PBF_ERR_DEVICE if the last
+ * pbf_op_sort_cells with this scratch, n and ncells had its look-back wait
+ * give up (its output is then void). */
+int pbf_op_sort_cells_status(const void *d_scratch, uint32_t n, uint32_t ncells, void *stream);
 /* CSR cell offsets of sorted keys: d_offsets[c] = number of keys < c for
  * c in [0, ncells]; every key must be < ncells. */
 int pbf_op_cell_offsets(const uint32_t *d_sorted_keys, uint32_t n,

@@ -114,11 +114,12 @@ class Tuning(C.Structure):
 
     PASSES = ("nbr_build", "nbr_lambda", "lambda", "delta", "vorticity", "xsph_commit")
     _fields_ = [("threads", C.c_uint32 * 6), ("batch", C.c_uint32 * 6), ("fuse_first", C.c_uint32),
-                ("trial_ms", C.c_float * 6), ("staged", C.c_uint32)]
+                ("trial_ms", C.c_float * 6), ("staged", C.c_uint32), ("radix_sort", C.c_uint32)]
 
     def as_dict(self) -> dict:
         return {"threads": dict(zip(self.PASSES, self.threads)), "batch": dict(zip(self.PASSES, self.batch)),
                 "fuse_first": int(self.fuse_first), "staged": int(self.staged),
+                "radix_sort": int(self.radix_sort),
                 "trial_ms": dict(zip(self.PASSES, self.trial_ms))}
 
 
@@ -213,6 +214,9 @@ def lib():
             "pbf_op_sort_pairs": ([vp, vp, u32, u32, vp, vp, vp, C.c_size_t, vp], i32),
             "pbf_op_sort_status": ([vp, u32, u32, vp], i32),
             "pbf_op_sort_pairs_noalloc": ([vp, vp, u32, u32, vp, vp, vp, vp], i32),
+            "pbf_op_sort_cells_scratch_bytes": ([u32, u32], C.c_size_t),
+            "pbf_op_sort_cells": ([vp, u32, u32, vp, vp, vp, vp, C.c_size_t, vp], i32),
+            "pbf_op_sort_cells_status": ([vp, u32, u32, vp], i32),
             "pbf_op_cell_offsets": ([vp, u32, u32, vp, vp], i32),
             "pbf_op_find_cells": ([vp, u32, vp, vp], i32),
             "pbf_selftest_bounded_wait": ([u32, C.POINTER(u32)], i32),
@@ -752,6 +756,20 @@ def op_sort_pairs(d_keys_in: int, d_vals_in, n: int, key_bits: int, d_keys_out: 
 
 def op_sort_status(d_scratch: int, n: int, key_bits: int, stream: int = 0):
     _check(lib().pbf_op_sort_status(d_scratch, n, key_bits, stream), "pbf_op_sort_status")
+
+
+def op_sort_cells_scratch_bytes(n: int, ncells: int) -> int:
+    return int(lib().pbf_op_sort_cells_scratch_bytes(n, ncells))
+
+
+def op_sort_cells(d_keys: int, n: int, ncells: int, d_offsets: int, d_sorted_keys: int, d_perm: int,
+                  d_scratch: int, scratch_bytes: int, stream: int = 0):
+    _check(lib().pbf_op_sort_cells(d_keys, n, ncells, d_offsets, d_sorted_keys, d_perm, d_scratch,
+                                   scratch_bytes, stream), "pbf_op_sort_cells")
+
+
+def op_sort_cells_status(d_scratch: int, n: int, ncells: int, stream: int = 0):
+    _check(lib().pbf_op_sort_cells_status(d_scratch, n, ncells, stream), "pbf_op_sort_cells_status")
 
 
 def op_cell_offsets(d_sorted_keys: int, n: int, ncells: int, d_offsets: int, stream: int = 0):

@@ -65,6 +65,7 @@ struct pbf_batch {
   uint32_t next_id = 0;
   uint32_t n_total = 0, cells_total = 0;
   SortPlan plan;
+  CellSortPlan cplan_cap, cplan;  // counting sort: layout at capacity, sizes of the layout
   bool dirty = true;
   // a step (or the tuner's trial steps) ran on the current layout, so the
   // neighbour lists and counts belong to it
@@ -122,6 +123,7 @@ int apply_layout(pbf_batch *b) {
   d.blk_total = blocks;
   b->pc.n = p;
   b->plan = make_sort_plan(p, bits_for(std::max<uint32_t>(c, 1)));
+  b->cplan = resize_cell_sort_plan(b->cplan_cap, p, c);
   if (!b->scenes.empty()) {
     PBF_TRY(cudaMemcpyAsync(d.scenes, b->table.data(), b->table.size() * sizeof(SceneDesc),
                             cudaMemcpyHostToDevice, b->stream));
@@ -138,12 +140,20 @@ int launch_batch_step(pbf_batch *b) {
   const cudaStream_t st = b->stream;
   const uint32_t n = b->n_total;
   const PaperConsts &pc = b->pc;
-  PBF_TRY(sort_clear(b->plan, d.sort_scratch, st));
-  PBF_TRY(paper_predict_hash(d.X, d.V, n, pc, d.scenes, d.sid, d.keys, b->plan, d.sort_scratch,
+  if (!d.tune.radix_sort) {
+    PBF_TRY(cell_sort_clear(b->cplan, d.cell_scratch, false, st));
+    PBF_TRY(paper_predict_count(d.X, d.V, n, pc, d.scenes, d.sid, d.keys, b->cplan,
+                                d.cell_scratch, st));
+    PBF_TRY(cell_sort_finish(b->cplan, d.keys, d.cell_scratch, d.offsets, d.skeys, d.perm, d.err,
                              st));
-  PBF_TRY(sort_scan(b->plan, d.sort_scratch, st));
-  PBF_TRY(sort_passes(b->plan, d.keys, nullptr, d.skeys, d.perm, d.sort_scratch, d.err, st));
-  PBF_TRY(cell_offsets_runs(d.skeys, n, b->cells_total, d.offsets, d.runs, d.runs_count, st));
+  } else {
+    PBF_TRY(sort_clear(b->plan, d.sort_scratch, st));
+    PBF_TRY(paper_predict_hash(d.X, d.V, n, pc, d.scenes, d.sid, d.keys, b->plan,
+                               d.sort_scratch, st));
+    PBF_TRY(sort_scan(b->plan, d.sort_scratch, st));
+    PBF_TRY(sort_passes(b->plan, d.keys, nullptr, d.skeys, d.perm, d.sort_scratch, d.err, st));
+    PBF_TRY(cell_offsets_runs(d.skeys, n, b->cells_total, d.offsets, d.runs, d.runs_count, st));
+  }
   PBF_TRY(paper_reorder(d.perm, d.X, d.V, d.ID, n, pc, d.X2, d.V2, d.ID2, d.P, d.D, st));
   const uint32_t iters = b->solver.solver_iterations;
   if (d.tune.staged) {
@@ -224,6 +234,7 @@ size_t pbf_batch_device_bytes(const pbf_params *solver, uint32_t max_scenes,
          (size_t)max_cells * sizeof(uint32_t) + 3 * sizeof(uint32_t) +  // cell-block list
          (size_t)offset_runs_capacity(max_cells) * sizeof(uint4) + sizeof(uint32_t) +
          sort_words_max(max_particles) * sizeof(uint32_t) +
+         make_cell_sort_plan(max_particles, max_cells).words * sizeof(uint32_t) +
          (size_t)max_scenes * sizeof(SceneDesc) + 64;
 }
 
@@ -274,6 +285,9 @@ int pbf_batch_create(const pbf_params *solver, uint32_t max_scenes, uint32_t max
   A(&d.runs, offset_runs_capacity(max_cells));
   A(&d.runs_count, 1);
   A(&d.sort_scratch, sort_words_max(max_particles));
+  b->cplan_cap = make_cell_sort_plan(max_particles, max_cells);
+  b->cplan = resize_cell_sort_plan(b->cplan_cap, 0, 0);
+  A(&d.cell_scratch, b->cplan_cap.words);
   A(&d.scenes, max_scenes);
   A(&d.err, 1);
   if (rc == PBF_OK) {
@@ -285,6 +299,7 @@ int pbf_batch_create(const pbf_params *solver, uint32_t max_scenes, uint32_t max
     return rc;
   }
   e = cudaMemsetAsync(d.err, 0, sizeof(uint32_t), b->stream);
+  if (e == cudaSuccess) e = cell_sort_clear(b->cplan_cap, d.cell_scratch, true, b->stream);
   if (e == cudaSuccess)
     e = cudaMemsetAsync(d.offsets, 0, ((size_t)max_cells + 1) * sizeof(uint32_t), b->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
@@ -465,7 +480,10 @@ int pbf_batch_launches_per_step(const pbf_batch *b, uint32_t *launches) {
   if (!b || !launches) return PBF_ERR_INVALID;
   const SortPlan plan = make_sort_plan(std::max<uint32_t>(b->n_total, 1),
                                        bits_for(std::max<uint32_t>(b->cells_total, 1)));
-  *launches = 1u + 1u + plan.passes + 2u + 1u + paper_first_launches(b->d) +
+  // predict + hash, the sort (counting: 4 launches; radix: scan, digit
+  // passes, two for the offsets), reorder, the solver, the velocity passes
+  const uint32_t sort = b->d.tune.radix_sort ? 1u + plan.passes + 2u : cell_sort_launches();
+  *launches = 1u + sort + 1u + paper_first_launches(b->d) +
               2u * b->solver.solver_iterations - 1u + 2u;
   return PBF_OK;
 }

@@ -37,4 +37,19 @@ __device__ __forceinline__ void warp_digit_histogram(uint32_t key, bool valid,
   }
 }
 
+// Counts key into counts[] for the counting sort: equal keys of a warp
+// aggregated into one atomic; pos[i] = the particle's place among the
+// increments of its cell (warp lanes in order, warps in atomic order).
+__device__ __forceinline__ void count_cell_key(uint32_t key, bool valid, uint32_t i,
+                                               uint32_t *__restrict__ counts,
+                                               uint32_t *__restrict__ pos) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const unsigned peers = __match_any_sync(0xffffffffu, valid ? key : 0xffffffffu);
+  const uint32_t leader = (uint32_t)(__ffs(peers) - 1);
+  uint32_t base = 0;
+  if (valid && lane == leader) base = atomicAdd(&counts[key], (uint32_t)__popc(peers));
+  base = __shfl_sync(0xffffffffu, base, (int)leader);
+  if (valid) pos[i] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+}
+
 }  // namespace pbf

@@ -13,8 +13,9 @@ namespace pbf {
 // Device-side error bits, OR-ed into a per-simulation flag word that the
 // host reads back at synchronisation points.
 enum DeviceError : uint32_t {
-  kDevErrLookback = 1u,  // a radix-sort look-back wait hit its bound
+  kDevErrLookback = 1u,  // a sort's look-back wait hit its bound
   kDevErrStage = 2u,     // a tile's bulk copies did not complete within the bounded wait
+  kDevErrKey = 4u,       // the cell-sort operator got a key not below its cell count
 };
 
 // ------------------------------------------------------------ grid / scene --
@@ -176,6 +177,46 @@ cudaError_t wait_selftest(uint32_t *scratch, uint32_t spin_limit, uint32_t *err,
 // Number of kernel launches of one sort (histogram not included).
 uint32_t sort_pass_launches(const SortPlan &plan);
 
+// Counting sort of cell keys (paper path): the predict kernel counts every
+// cell's particles into `counts` and keeps each particle's place among its
+// cell's in `pos`; cell_sort_finish turns the counts into the cell offsets
+// (leaving the counts zero for the next step), scatters the particles and
+// puts each cell back in index order, so skeys / perm are the stable sort's.
+// Layout of its scratch (32-bit words):
+struct CellSortPlan {
+  uint32_t n = 0, ncells = 0, tiles = 0;
+  uint32_t big_cap = 0, huge_cap = 0;
+  uint32_t bm_words = 0;   // words of a bitmap over the n particle indices
+  uint32_t bm_stride = 0;  // words from one CTA's bitmap to the next
+  size_t off_counts = 0;  // ncells: per-cell counts (zero between steps)
+  size_t off_pos = 0;     // n: each particle's place among its cell's
+  size_t off_ctl = 0;     // [0] scan tiles started, [1] big cells, [2] huge cells, then
+  size_t ctl_words = 0;   //     the scan's look-back words (zeroed before every step)
+  size_t off_big = 0;     // cells of 17..8192 particles
+  size_t off_huge = 0;    // cells of more than 8192
+  size_t off_bitmap = 0;  // one bitmap of the particle indices per huge-cell CTA
+  size_t words = 0;
+};
+CellSortPlan make_cell_sort_plan(uint32_t n, uint32_t ncells);
+// The same layout (sized for n_cap particles and cells_cap cells) sorting
+// n particles over ncells cells: a batch keeps one layout of its scratch
+// while its scenes change.
+CellSortPlan resize_cell_sort_plan(const CellSortPlan &cap, uint32_t n, uint32_t ncells);
+// Zeroes the control words (and, with counts = true, the counts: once after
+// allocation).
+cudaError_t cell_sort_clear(const CellSortPlan &plan, uint32_t *scratch, bool counts,
+                            cudaStream_t stream);
+// Offsets, scatter and in-cell order after the predict kernel has counted
+// (4 launches).
+cudaError_t cell_sort_finish(const CellSortPlan &plan, const uint32_t *keys, uint32_t *scratch,
+                             uint32_t *offsets, uint32_t *skeys, uint32_t *perm, uint32_t *err,
+                             cudaStream_t stream);
+uint32_t cell_sort_launches();
+// The predict kernel's counting from a key array; a key outside
+// [0, plan.ncells) is left out and sets kDevErrKey in *err.
+cudaError_t cell_sort_count(const CellSortPlan &plan, const uint32_t *keys, uint32_t *scratch,
+                            uint32_t *err, cudaStream_t stream);
+
 // ------------------------------------------------- gather-pass launch shape --
 // The gather passes of the paper equations, as tuned separately.
 enum GatherKind : int {
@@ -200,6 +241,9 @@ struct GatherTuning {
   // 1: the gather passes stage each tile's neighbourhood in shared memory
   // (pbf_tile.cu; one 128-thread shape, fuse_first does not apply)
   uint8_t staged = 0;
+  // 1: the onesweep radix sort of the cell keys instead of the counting
+  // sort by cell (same permutation)
+  uint8_t radix_sort = 0;
 };
 constexpr int kBlockCodes = 3;  // 64, 128, 256
 constexpr int kBatchCodes = 2;  // 4, 8
@@ -278,6 +322,7 @@ struct DeviceState {
   uint32_t *nbr_cnt = nullptr;         // neighbour counts (paper)
   uint32_t *nbr_max = nullptr;         // largest neighbour count of the step (paper)
   uint32_t *sort_scratch = nullptr;
+  uint32_t *cell_scratch = nullptr;    // counting sort by cell (paper)
   uint32_t *err = nullptr;             // device error flag word
   SceneDesc *scenes = nullptr;         // device scene table
   float4 *io_pos = nullptr, *io_vel = nullptr; // input-order staging
@@ -341,6 +386,12 @@ cudaError_t paper_predict_hash(const float4 *X, const float4 *V, uint32_t n,
                                const uint16_t *sid, uint32_t *keys,
                                const SortPlan &plan, uint32_t *sort_scratch,
                                cudaStream_t st);
+// The same prediction and keys, counted for the counting sort.
+cudaError_t paper_predict_count(const float4 *X, const float4 *V, uint32_t n,
+                                const PaperConsts &c, const SceneDesc *scenes,
+                                const uint16_t *sid, uint32_t *keys,
+                                const CellSortPlan &plan, uint32_t *cell_scratch,
+                                cudaStream_t st);
 cudaError_t paper_reorder(const uint32_t *perm, const float4 *X,
                           const float4 *V, const uint32_t *ID, uint32_t n,
                           const PaperConsts &c, float4 *X2, float4 *V2,

@@ -62,6 +62,30 @@ namespace {
 
 
 // ------------------------------------------------------------------------
+// Prediction and cell key of every particle (grid-stride, whole warps
+// iterate together), counted for the counting sort.
+__global__ void __launch_bounds__(256)
+    k_predict_count(const float4 *__restrict__ X, const float4 *__restrict__ V, uint32_t n,
+                    PaperConsts c, const SceneDesc *__restrict__ scenes,
+                    const uint16_t *__restrict__ sid, uint32_t *__restrict__ keys,
+                    uint32_t *__restrict__ counts, uint32_t *__restrict__ pos) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t k = base + threadIdx.x;
+    const bool valid = k < n;
+    uint32_t key = 0;
+    if (valid) {
+      const float4 x = X[k];
+      const float4 v1 = gravity_velocity(V[k], c.dt, c.gy);
+      const float3 p = add3(x, displacement(v1, c.dt));
+      const SceneDesc &s = scene_of(scenes, sid, k);
+      key = s.cell_base + scene_cell(p.x, p.y, p.z, s);
+      keys[k] = key;
+    }
+    count_cell_key(key, valid, k, counts, pos);
+  }
+}
+
 __global__ void __launch_bounds__(256)
     k_predict_hash(const float4 *__restrict__ X, const float4 *__restrict__ V,
                    uint32_t n, PaperConsts c,
@@ -323,6 +347,17 @@ cudaError_t paper_predict_hash(const float4 *X, const float4 *V, uint32_t n,
   k_predict_hash<<<min(blocks_for(n, 256), kStrideCtas), 256, 0, st>>>(
       X, V, n, c, scenes, sid, keys, plan.passes, plan.digit_bits,
       sort_scratch + plan.off_hist);
+  return cudaGetLastError();
+}
+
+cudaError_t paper_predict_count(const float4 *X, const float4 *V, uint32_t n,
+                                const PaperConsts &c, const SceneDesc *scenes,
+                                const uint16_t *sid, uint32_t *keys,
+                                const CellSortPlan &plan, uint32_t *cell_scratch,
+                                cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_predict_count<<<min(blocks_for(n, 256), kStrideCtas), 256, 0, st>>>(
+      X, V, n, c, scenes, sid, keys, cell_scratch + plan.off_counts, cell_scratch + plan.off_pos);
   return cudaGetLastError();
 }
 

@@ -240,6 +240,7 @@ void to_pbf_tuning(const GatherTuning &g, const double trial_ms[kGatherKinds], p
   }
   out->fuse_first = g.fuse_first;
   out->staged = g.staged;
+  out->radix_sort = g.radix_sort;
 }
 
 int to_gather_tuning(const pbf_tuning &t, GatherTuning *out) {
@@ -267,6 +268,11 @@ int to_gather_tuning(const pbf_tuning &t, GatherTuning *out) {
     return PBF_ERR_INVALID;
   }
   g.staged = (uint8_t)t.staged;
+  if (t.radix_sort > 1) {
+    set_error_message("tuning: radix_sort must be 0 or 1");
+    return PBF_ERR_INVALID;
+  }
+  g.radix_sort = (uint8_t)t.radix_sort;
   *out = g;
   return PBF_OK;
 }

@@ -42,6 +42,7 @@ struct pbf_sim {
   RefConsts rc{};
   SceneDesc scene{};
   SortPlan plan;
+  CellSortPlan cplan;  // paper mode's counting sort
   uint32_t ncells = 0;
   std::vector<void *> allocations;
   size_t device_bytes = 0;
@@ -188,8 +189,19 @@ int launch_step(pbf_sim *s) {
   size_t ev = 0;
   s->events_used = 0;
   PBF_TRY_STATUS(mark(s, -1, "start", 0, &ev));
-  PBF_TRY(sort_clear(s->plan, d.sort_scratch, st));
-  if (s->paper) {
+  if (s->paper && !d.tune.radix_sort) {
+    // counting sort by cell: the counts, the offsets, the scatter and the
+    // order within each cell
+    PBF_TRY(cell_sort_clear(s->cplan, d.cell_scratch, false, st));
+    PBF_TRY(cudaMemsetAsync(d.nbr_max, 0, sizeof(uint32_t), st));
+    PBF_TRY(paper_predict_count(d.X, d.V, n, s->pc, d.scenes, nullptr, d.keys, s->cplan,
+                                d.cell_scratch, st));
+    PBF_TRY_STATUS(mark(s, 0, "predict_hash", 1, &ev));
+    PBF_TRY(cell_sort_finish(s->cplan, d.keys, d.cell_scratch, d.offsets, d.skeys, d.perm, d.err,
+                             st));
+    PBF_TRY_STATUS(mark(s, 0, "cell_sort", cell_sort_launches(), &ev));
+  } else if (s->paper) {
+    PBF_TRY(sort_clear(s->plan, d.sort_scratch, st));
     PBF_TRY(cudaMemsetAsync(d.nbr_max, 0, sizeof(uint32_t), st));
     PBF_TRY(paper_predict_hash(d.X, d.V, n, s->pc, d.scenes, nullptr, d.keys,
                                s->plan, d.sort_scratch, st));
@@ -200,6 +212,10 @@ int launch_step(pbf_sim *s) {
     PBF_TRY_STATUS(mark(s, 0, "sort_onesweep", 1 + passes, &ev));
     PBF_TRY(step_offsets(s));
     PBF_TRY_STATUS(mark(s, 0, "cell_offsets", 1, &ev));
+  } else {
+    PBF_TRY(sort_clear(s->plan, d.sort_scratch, st));
+  }
+  if (s->paper) {
     PBF_TRY(paper_reorder(d.perm, d.X, d.V, d.ID, n, s->pc, d.X2, d.V2, d.ID2,
                           d.P, d.D, st));
     PBF_TRY_STATUS(mark(s, 0, "reorder", 1, &ev));
@@ -438,6 +454,7 @@ int pbf_create(const pbf_params *params, const pbf_particle *particles,
   s->rc.n = n;
   s->pc = make_paper_consts(*params, n);
   s->plan = make_sort_plan(n, bits_for(s->ncells));
+  s->cplan = make_cell_sort_plan(n, s->ncells);
   *out = s.release();
   return PBF_OK;
 }
@@ -483,6 +500,7 @@ int pbf_init(pbf_sim *s) {
     A(&d.R, n);
     A(&d.nbr_cnt, n);
     A(&d.nbr_max, 1);
+    A(&d.cell_scratch, s->cplan.words);
     A(&d.nbr, (size_t)paper_list_words(s->pc.maxn) * n);
     d.blk_total = d.blk_cap = scene_blocks(s->scene);
     A(&d.blk_list, d.blk_cap);
@@ -517,6 +535,7 @@ int pbf_init(pbf_sim *s) {
     vel[i] = make_float4(p.v[0], p.v[1], p.v[2], p.m);
   }
   PBF_TRY(cudaMemsetAsync(d.err, 0, sizeof(uint32_t), s->stream));
+  if (s->paper) PBF_TRY(cell_sort_clear(s->cplan, d.cell_scratch, true, s->stream));
   PBF_TRY(cudaMemsetAsync(d.P, 0, n * sizeof(float4), s->stream));
   PBF_TRY(cudaMemsetAsync(d.offsets, 0, ((size_t)s->ncells + 1) * sizeof(uint32_t),
                           s->stream));
@@ -700,7 +719,9 @@ int pbf_set_graph(pbf_sim *s, int enable) {
 int pbf_launches_per_step(const pbf_sim *s, uint32_t *launches) {
   if (!s || !launches) return PBF_ERR_INVALID;
   const uint32_t it = s->prm.solver_iterations;
-  const uint32_t sort = 1u /*scan*/ + s->plan.passes + (s->offset_runs ? 2u : 1u) /*offsets*/;
+  const uint32_t sort = s->paper && !s->d.tune.radix_sort
+                            ? cell_sort_launches()
+                            : 1u /*scan*/ + s->plan.passes + (s->offset_runs ? 2u : 1u) /*offsets*/;
   if (s->paper)
     *launches = 1u /*predict+hash*/ + sort + 1u /*reorder*/ + paper_first_launches(s->d) +
                 2u * it - 1u + 2u;
@@ -876,6 +897,43 @@ int pbf_op_sort_status(const void *d_scratch, uint32_t n, uint32_t key_bits,
   PBF_TRY(cudaStreamSynchronize((cudaStream_t)stream));
   if (flag) {
     set_error_message("radix sort look-back wait gave up");
+    return PBF_ERR_DEVICE;
+  }
+  return PBF_OK;
+}
+
+size_t pbf_op_sort_cells_scratch_bytes(uint32_t n, uint32_t ncells) {
+  return make_cell_sort_plan(n, ncells).words * sizeof(uint32_t);
+}
+
+int pbf_op_sort_cells(const uint32_t *d_keys, uint32_t n, uint32_t ncells, uint32_t *d_offsets,
+                      uint32_t *d_sorted_keys, uint32_t *d_perm, void *d_scratch,
+                      size_t scratch_bytes, void *stream) {
+  if (ncells == 0 || !d_offsets || !d_scratch) return PBF_ERR_INVALID;
+  if (n && (!d_keys || !d_sorted_keys || !d_perm)) return PBF_ERR_INVALID;
+  if (n >= (1u << 30)) return PBF_ERR_INVALID;
+  const CellSortPlan plan = make_cell_sort_plan(n, ncells);
+  if (scratch_bytes < plan.words * sizeof(uint32_t)) return PBF_ERR_INVALID;
+  uint32_t *scratch = static_cast<uint32_t *>(d_scratch);
+  const cudaStream_t st = (cudaStream_t)stream;
+  // the control words hold the error word (ctl[3]); the counts start at zero
+  PBF_TRY(cell_sort_clear(plan, scratch, true, st));
+  PBF_TRY(cell_sort_count(plan, d_keys, scratch, scratch + plan.off_ctl + 3, st));
+  PBF_TRY(cell_sort_finish(plan, d_keys, scratch, d_offsets, d_sorted_keys, d_perm,
+                           scratch + plan.off_ctl + 3, st));
+  return PBF_OK;
+}
+
+int pbf_op_sort_cells_status(const void *d_scratch, uint32_t n, uint32_t ncells, void *stream) {
+  if (!d_scratch || ncells == 0) return PBF_ERR_INVALID;
+  const CellSortPlan plan = make_cell_sort_plan(n, ncells);
+  uint32_t flag = 0;
+  const uint32_t *err = static_cast<const uint32_t *>(d_scratch) + plan.off_ctl + 3;
+  PBF_TRY(cudaMemcpyAsync(&flag, err, 4, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  PBF_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  if (flag) {
+    set_error_message(flag & kDevErrKey ? "cell sort: a key not below ncells"
+                                        : "cell sort look-back wait gave up");
     return PBF_ERR_DEVICE;
   }
   return PBF_OK;

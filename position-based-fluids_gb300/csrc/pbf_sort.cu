@@ -21,6 +21,7 @@
 // counter in the order CTAs start, so a CTA only ever waits on tiles that
 // are already resident; every wait is additionally bounded, and a wait that
 // runs out sets a device error bit instead of spinning on.
+#include <algorithm>
 #include <mutex>
 
 #include "pbf_device.cuh"
@@ -399,6 +400,269 @@ inline uint32_t blocks_for(uint64_t n, uint32_t t) {
   return (uint32_t)((n + t - 1) / t);
 }
 
+// ------------------------------------------------- counting sort by cell --
+// The cell keys of a step sorted in one pass: the predict kernel counts each
+// cell's particles (count_cell_key: warp-aggregated atomics, each particle
+// keeping its place among the increments of its cell), k_count_scan turns
+// the counts into the cell offsets (and zeroes them for the next step),
+// k_count_scatter puts every particle at its cell's offset plus its place,
+// and the cells are then put back in index order -- the order a stable sort
+// gives -- because the places of particles counted by different warps
+// follow the order of their atomics: k_cell_fix sorts cells of up to 16
+// particles in registers and lists the larger ones, k_cell_fix_big sorts
+// those of up to kBigCell in shared memory (one CTA per cell) and larger
+// ones through a per-CTA bitmap of the particle indices.
+constexpr uint32_t kScanItems = 8;
+constexpr uint32_t kScanTile = kSortThreads * kScanItems;  // counts per scan tile
+constexpr uint32_t kSmallCell = 16;
+constexpr uint32_t kBigCell = 8192;
+
+// Exclusive prefix of tile `tile` from the look-back words of the tiles
+// before it, 32 tiles per round (lane l reads tile t - l; the nearest
+// inclusive word ends the walk).  Runs on one full warp; a wait of more than
+// spin_limit polls sets kDevErrLookback in *err and gives up.
+__device__ __forceinline__ uint32_t warp_lookback(uint32_t *lookback, uint32_t tile,
+                                                  uint32_t spin_limit, uint32_t *err) {
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t excl = 0;
+  int t = (int)tile - 1;
+  while (t >= 0) {
+    const int p = t - (int)lane;
+    uint32_t v = p >= 0 ? ld_volatile(&lookback[p]) : kLbInclusive;
+    uint32_t spins = 0;
+    bool gave_up = false;
+    while (!__all_sync(0xffffffffu, (v & ~kLbMask) != 0u)) {
+      if ((v & ~kLbMask) == 0u) v = ld_volatile(&lookback[p]);
+      if (++spins >= spin_limit) {
+        gave_up = true;
+        break;
+      }
+      if (spins > 64) __nanosleep(32);
+    }
+    if (gave_up) {
+      if (lane == 0) atomicOr(err, kDevErrLookback);
+      break;
+    }
+    const unsigned inc = __ballot_sync(0xffffffffu, (v & ~kLbMask) == kLbInclusive);
+    const uint32_t stop = inc ? (uint32_t)(__ffs(inc) - 1) : 31u;
+    uint32_t part = lane <= stop ? (v & kLbMask) : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    excl += part;
+    if (inc) break;
+    t -= 32;
+  }
+  return excl;
+}
+
+// off[c] = particles in cells below c, for c in [0, ncells]; counts[c] -> 0.
+// Tiles of kScanTile counts are numbered in the order CTAs start.
+__global__ void __launch_bounds__(kSortThreads)
+    k_count_scan(uint32_t *__restrict__ counts, uint32_t ncells, uint32_t total,
+                 uint32_t *__restrict__ off, uint32_t *ctl, uint32_t *err) {
+  __shared__ uint32_t s_tile, s_total, s_excl;
+  __shared__ uint32_t s_warp[kSortWarps];
+  uint32_t *lookback = ctl + 4;
+  const uint32_t tid = threadIdx.x;
+  if (tid == 0) s_tile = atomicAdd(&ctl[0], 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint32_t base = tile * kScanTile + tid * kScanItems;
+  uint32_t v[kScanItems], sum = 0;
+#pragma unroll
+  for (uint32_t j = 0; j < kScanItems; ++j) {
+    const uint32_t idx = base + j;
+    v[j] = idx < ncells ? counts[idx] : 0u;
+    sum += v[j];
+  }
+#pragma unroll
+  for (uint32_t j = 0; j < kScanItems; ++j)
+    if (v[j]) counts[base + j] = 0u;
+  const uint32_t texcl = block_exclusive_scan(sum, s_warp);
+  if (tid == kSortThreads - 1) s_total = texcl + sum;
+  __syncthreads();
+  if (tid < 32) {
+    const uint32_t tot = s_total;
+    if (tile == 0) {
+      if (tid == 0) {
+        st_volatile(&lookback[0], kLbInclusive | tot);
+        s_excl = 0;
+        off[ncells] = total;
+      }
+    } else {
+      if (tid == 0) st_volatile(&lookback[tile], kLbAggregate | tot);
+      __syncwarp();
+      const uint32_t excl = warp_lookback(lookback, tile, kSpinLimit, err);
+      if (tid == 0) {
+        st_volatile(&lookback[tile], kLbInclusive | ((excl + tot) & kLbMask));
+        s_excl = excl;
+      }
+    }
+  }
+  __syncthreads();
+  uint32_t run = s_excl + texcl;
+#pragma unroll
+  for (uint32_t j = 0; j < kScanItems; ++j) {
+    const uint32_t idx = base + j;
+    if (idx < ncells) off[idx] = run;
+    run += v[j];
+  }
+}
+
+// The counting of the predict kernel, from a key array (the operator).
+// A key outside [0, ncells) is not counted and sets kDevErrKey in *err.
+__global__ void __launch_bounds__(256)
+    k_count_keys(const uint32_t *__restrict__ keys, uint32_t n, uint32_t ncells,
+                 uint32_t *__restrict__ counts, uint32_t *__restrict__ pos, uint32_t *err) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t key = i < n ? keys[i] : 0u;
+    const bool valid = i < n && key < ncells;
+    if (i < n && !valid) atomicOr(err, kDevErrKey);
+    count_cell_key(key, valid, i, counts, pos);
+  }
+}
+
+// Every particle at its cell's offset plus its place among the cell's.
+__global__ void __launch_bounds__(256)
+    k_count_scatter(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ pos,
+                    const uint32_t *__restrict__ off, uint32_t n, uint32_t ncells,
+                    uint32_t *__restrict__ skeys, uint32_t *__restrict__ perm) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t k = keys[i];
+  if (k >= ncells) return;  // not counted (error flag set)
+  const uint32_t d = off[k] + pos[i];
+  // always true unless the scan's look-back gave up (error flag set)
+  if (d < n) {
+    skeys[d] = k;
+    perm[d] = i;
+  }
+}
+
+// One thread per cell: a cell of up to kSmallCell particles sorted by index
+// in registers (bitonic network, only when out of order); larger cells
+// listed for k_cell_fix_big.
+__global__ void __launch_bounds__(256)
+    k_cell_fix(const uint32_t *__restrict__ off, uint32_t ncells, uint32_t *__restrict__ perm,
+               uint32_t *__restrict__ big, uint32_t big_cap, uint32_t *__restrict__ huge,
+               uint32_t huge_cap, uint32_t *ctl) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const uint32_t a = off[c], m = off[c + 1] - a;
+  if (m <= 1u) return;
+  if (m > kSmallCell) {
+    if (m <= kBigCell) {
+      const uint32_t q = atomicAdd(&ctl[1], 1u);
+      if (q < big_cap) big[q] = c;
+    } else {
+      const uint32_t q = atomicAdd(&ctl[2], 1u);
+      if (q < huge_cap) huge[q] = c;
+    }
+    return;
+  }
+  uint32_t v[kSmallCell];
+  bool sorted = true;
+#pragma unroll
+  for (uint32_t j = 0; j < kSmallCell; ++j) {
+    v[j] = j < m ? perm[a + j] : 0xffffffffu;
+    if (j > 0 && j < m && v[j] < v[j - 1]) sorted = false;
+  }
+  if (sorted) return;
+#pragma unroll
+  for (uint32_t k = 2; k <= kSmallCell; k <<= 1)
+#pragma unroll
+    for (uint32_t j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+      for (uint32_t i = 0; i < kSmallCell; ++i) {
+        const uint32_t l = i ^ j;
+        if (l > i) {
+          const uint32_t x = v[i], y = v[l];
+          const uint32_t lo = min(x, y), hi = max(x, y);
+          const bool up = (i & k) == 0u;
+          v[i] = up ? lo : hi;
+          v[l] = up ? hi : lo;
+        }
+      }
+#pragma unroll
+  for (uint32_t j = 0; j < kSmallCell; ++j)
+    if (j < m) perm[a + j] = v[j];
+}
+
+constexpr uint32_t kHugeCtas = 4;  // CTAs that take the huge cells (one bitmap each)
+
+// The listed cells: up to kBigCell particles sorted in shared memory (one
+// CTA per cell, bitonic); more through a bitmap of the particle indices
+// (bm_words words per CTA, kHugeCtas CTAs): mark every index of the cell,
+// then write the marked indices in ascending order.
+__global__ void __launch_bounds__(kSortThreads)
+    k_cell_fix_big(const uint32_t *__restrict__ off, uint32_t *__restrict__ perm,
+                   const uint32_t *__restrict__ big, uint32_t big_cap,
+                   const uint32_t *__restrict__ huge, uint32_t huge_cap, const uint32_t *ctl,
+                   uint32_t *__restrict__ bitmap, uint32_t bm_words, uint32_t bm_stride) {
+  __shared__ uint32_t s[kBigCell];
+  __shared__ uint32_t s_warp[kSortWarps];
+  __shared__ uint32_t s_total;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t nbig = min(ctl[1], big_cap), nhuge = min(ctl[2], huge_cap);
+  for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
+    const uint32_t c = big[b];
+    const uint32_t a = off[c], m = off[c + 1] - a;
+    uint32_t P = 1;
+    while (P < m) P <<= 1;
+    for (uint32_t i = tid; i < P; i += kSortThreads) s[i] = i < m ? perm[a + i] : 0xffffffffu;
+    __syncthreads();
+    for (uint32_t k = 2; k <= P; k <<= 1)
+      for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+        for (uint32_t i = tid; i < P; i += kSortThreads) {
+          const uint32_t l = i ^ j;
+          if (l > i) {
+            const uint32_t x = s[i], y = s[l];
+            const bool up = (i & k) == 0u;
+            if ((x > y) == up) {
+              s[i] = y;
+              s[l] = x;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    for (uint32_t i = tid; i < m; i += kSortThreads) perm[a + i] = s[i];
+    __syncthreads();
+  }
+  if (blockIdx.x >= kHugeCtas) return;
+  uint32_t *bm = bitmap + (size_t)blockIdx.x * bm_stride;
+  for (uint32_t h = blockIdx.x; h < nhuge; h += kHugeCtas) {
+    const uint32_t c = huge[h];
+    const uint32_t a = off[c], m = off[c + 1] - a;
+    for (uint32_t w = tid; w < bm_words; w += kSortThreads) bm[w] = 0u;
+    __syncthreads();
+    for (uint32_t i = tid; i < m; i += kSortThreads) {
+      const uint32_t x = perm[a + i];
+      atomicOr(&bm[x >> 5], 1u << (x & 31u));
+    }
+    __syncthreads();
+    uint32_t carry = 0;
+    for (uint32_t w0 = 0; w0 < bm_words; w0 += kSortThreads) {
+      const uint32_t w = w0 + tid;
+      uint32_t word = w < bm_words ? bm[w] : 0u;
+      const uint32_t cnt = (uint32_t)__popc(word);
+      uint32_t at = a + carry + block_exclusive_scan(cnt, s_warp);
+      if (tid == kSortThreads - 1) s_total = at - a - carry + cnt;
+      while (word) {
+        const uint32_t bit = (uint32_t)(__ffs(word) - 1);
+        if (at < a + m) perm[at] = (w << 5) + bit;
+        ++at;
+        word &= word - 1u;
+      }
+      __syncthreads();
+      carry += s_total;
+      __syncthreads();
+    }
+  }
+}
+
 }  // namespace
 
 uint32_t bits_for(uint32_t max_key_exclusive) {
@@ -518,6 +782,91 @@ cudaError_t cell_hash(const float4 *pred, uint32_t n, const SceneDesc &scene,
                       uint32_t *hash, cudaStream_t stream) {
   if (n == 0) return cudaSuccess;
   k_cell_hash<<<blocks_for(n, 256), 256, 0, stream>>>(pred, n, scene, hash);
+  return cudaGetLastError();
+}
+
+CellSortPlan make_cell_sort_plan(uint32_t n, uint32_t ncells) {
+  CellSortPlan p;
+  p.n = n;
+  p.ncells = ncells;
+  p.tiles = (uint32_t)(((uint64_t)ncells + kScanTile - 1) / kScanTile);
+  p.big_cap = (uint32_t)std::min<uint64_t>(ncells, (uint64_t)n / (kSmallCell + 1) + 1);
+  p.huge_cap = n / (kBigCell + 1) + 1;
+  p.bm_words = (n + 31u) / 32u;
+  p.bm_stride = p.bm_words;
+  size_t w = 0;
+  p.off_counts = w;
+  w += ncells;
+  w = (w + 63) & ~size_t(63);
+  p.off_pos = w;
+  w += n;
+  w = (w + 63) & ~size_t(63);
+  p.off_ctl = w;
+  p.ctl_words = 4 + (size_t)p.tiles;
+  w += p.ctl_words;
+  w = (w + 63) & ~size_t(63);
+  p.off_big = w;
+  w += p.big_cap;
+  p.off_huge = w;
+  w += p.huge_cap;
+  w = (w + 63) & ~size_t(63);
+  p.off_bitmap = w;
+  w += (size_t)kHugeCtas * p.bm_stride;
+  p.words = w;
+  return p;
+}
+
+CellSortPlan resize_cell_sort_plan(const CellSortPlan &cap, uint32_t n, uint32_t ncells) {
+  CellSortPlan p = cap;
+  p.n = std::min(n, cap.n);
+  p.ncells = std::min(ncells, cap.ncells);
+  p.tiles = (uint32_t)(((uint64_t)p.ncells + kScanTile - 1) / kScanTile);
+  p.ctl_words = 4 + (size_t)p.tiles;
+  p.bm_words = (p.n + 31u) / 32u;
+  return p;
+}
+
+cudaError_t cell_sort_clear(const CellSortPlan &plan, uint32_t *scratch, bool counts,
+                            cudaStream_t stream) {
+  if (counts) {
+    const cudaError_t e = cudaMemsetAsync(scratch + plan.off_counts, 0,
+                                          (size_t)plan.ncells * sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaMemsetAsync(scratch + plan.off_ctl, 0, plan.ctl_words * sizeof(uint32_t), stream);
+}
+
+cudaError_t cell_sort_finish(const CellSortPlan &plan, const uint32_t *keys, uint32_t *scratch,
+                             uint32_t *offsets, uint32_t *skeys, uint32_t *perm, uint32_t *err,
+                             cudaStream_t stream) {
+  uint32_t *ctl = scratch + plan.off_ctl;
+  if (plan.ncells == 0) return cudaErrorInvalidValue;
+  k_count_scan<<<plan.tiles, kSortThreads, 0, stream>>>(scratch + plan.off_counts, plan.ncells,
+                                                         plan.n, offsets, ctl, err);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || plan.n == 0) return e;
+  k_count_scatter<<<blocks_for(plan.n, 256), 256, 0, stream>>>(
+      keys, scratch + plan.off_pos, offsets, plan.n, plan.ncells, skeys, perm);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_cell_fix<<<blocks_for(plan.ncells, 256), 256, 0, stream>>>(
+      offsets, plan.ncells, perm, scratch + plan.off_big, plan.big_cap, scratch + plan.off_huge,
+      plan.huge_cap, ctl);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_cell_fix_big<<<kStrideCtas / 4u, kSortThreads, 0, stream>>>(
+      offsets, perm, scratch + plan.off_big, plan.big_cap, scratch + plan.off_huge,
+      plan.huge_cap, ctl, scratch + plan.off_bitmap, plan.bm_words, plan.bm_stride);
+  return cudaGetLastError();
+}
+
+uint32_t cell_sort_launches() { return 4u; }
+
+cudaError_t cell_sort_count(const CellSortPlan &plan, const uint32_t *keys, uint32_t *scratch,
+                            uint32_t *err, cudaStream_t stream) {
+  if (plan.n == 0) return cudaSuccess;
+  k_count_keys<<<min(blocks_for(plan.n, 256), kStrideCtas), 256, 0, stream>>>(
+      keys, plan.n, plan.ncells, scratch + plan.off_counts, scratch + plan.off_pos, err);
   return cudaGetLastError();
 }
 

@@ -34,6 +34,12 @@ def test_algorithmic_bytes_sum_to_the_step_total():
     assert bench.sort_bytes(cells_64) == bench.ALG_BYTES["sort_onesweep"] == 4 + 16 * 2
 
 
+def test_counting_sort_bytes():
+    n, cells = 1 << 20, 64 ** 3
+    assert bench.cell_sort_bytes(n, cells) == bench.ALG_BYTES["cell_sort"] == 22
+    assert bench.step_bytes(cells, n, counting=True) == 592 - 36 - 8 + 22
+
+
 def test_sort_passes_follow_the_digit_plan():
     # 9-bit digits only for 9 and 17-18 key bits; 8-bit digits otherwise
     want = {1: 1, 8: 1, 9: 1, 10: 2, 16: 2, 17: 2, 18: 2, 19: 3, 20: 3, 24: 3, 25: 4,

@@ -167,7 +167,7 @@ def test_stage_timing_reports_four_stages(pbf):
         timed = sim.dumpData()
         assert (ms > 0).all() and np.isfinite(ms).all()
         assert sim.launches_per_step() >= 10
-        assert {"predict_hash", "sort_onesweep", "reorder", "delta", "xsph_commit"} <= set(kt)
+        assert {"predict_hash", "cell_sort", "reorder", "delta", "xsph_commit"} <= set(kt)
         assert all(t > 0 for t, _ in kt.values())
     with pbf.Simulation(sc.params, sc.particles) as sim:
         sim.init()
