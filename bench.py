@@ -547,12 +547,14 @@ def run_ours(args) -> int:
     if args.load_state:
         sim.load_state(args.load_state)
     tuning = None if args.no_tune else sim.autotune(3).as_dict()
-    if args.first_pass != "auto" or args.staged != "auto":
+    if args.first_pass != "auto" or args.staged != "auto" or args.sort != "auto":
         t = sim.tuning()
         if args.first_pass != "auto":
             t.fuse_first = 1 if args.first_pass == "fused" else 0
         if args.staged != "auto":
             t.staged = 1 if args.staged == "on" else 0
+        if args.sort != "auto":
+            t.radix_sort = 1 if args.sort == "radix" else 0
         sim.set_tuning(t)
         tuning = sim.tuning().as_dict()
     ext = torch.cuda.ExternalStream(sim.stream())
@@ -698,7 +700,17 @@ def run_ours(args) -> int:
     return 0
 
 
-def plain_one_by_one(pbf, scenes, steps: int, sample_steps: int, ext_stream_of):
+def with_sort(obj, sort: str):
+    """Sets the step's cell sort of a simulation or batch ("counting" or
+    "radix"; "auto" keeps the library's default, the counting sort)."""
+    if sort != "auto":
+        t = obj.tuning()
+        t.radix_sort = 1 if sort == "radix" else 0
+        obj.set_tuning(t)
+    return obj
+
+
+def plain_one_by_one(pbf, scenes, steps: int, sample_steps: int, ext_stream_of, sort: str = "auto"):
     """The scenes solved one at a time on the plain path: per scene, create,
     upload, warm up, then time `sample_steps` graph-replayed steps with CUDA
     events.  Returns per-scene seconds for `steps` steps (sampled rate x
@@ -710,6 +722,7 @@ def plain_one_by_one(pbf, scenes, steps: int, sample_steps: int, ext_stream_of):
         w0 = time.perf_counter()
         sim = pbf.Simulation(s.params, s.particles)
         sim.init()
+        with_sort(sim, sort)
         sim.step(3)
         ext = ext_stream_of(sim)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -751,6 +764,8 @@ def run_batch(args, emit: bool = True):
     b = pbf.Batch(solver, len(scenes), n_tot, cells_tot)
     ids = [b.add_scene(s.params, s.particles) for s in scenes]
     tuning = None if args.no_tune else b.autotune(3).as_dict()
+    if args.sort != "auto":
+        tuning = with_sort(b, args.sort).tuning().as_dict()
     ext = torch.cuda.ExternalStream(b.stream())
     launches = b.launches_per_step()
     b.step(args.warmup)
@@ -784,7 +799,8 @@ def run_batch(args, emit: bool = True):
     if rank == 0 and not args.no_plain:
         sample = max(3, min(steps, args.plain_sample))
         plain_step_s, plain_setup_s = plain_one_by_one(
-            pbf, scenes, steps, sample, lambda sim: torch.cuda.ExternalStream(sim.stream()))
+            pbf, scenes, steps, sample, lambda sim: torch.cuda.ExternalStream(sim.stream()),
+            args.sort)
         t_plain = sum(plain_step_s)
         done = np.cumsum([a + c for a, c in zip(plain_step_s, plain_setup_s)])
         plain = {"value": n_tot * ITERATIONS * steps / t_plain, "unit": UNIT,
@@ -1084,6 +1100,10 @@ def main() -> int:
     ap.add_argument("--staged", choices=["auto", "on", "off"], default="auto",
                     help="single and large scenes: gather passes on staged shared-memory tiles, "
                          "through L1, or the tuner's (or default) choice")
+    ap.add_argument("--sort", choices=["auto", "counting", "radix"], default="auto",
+                    help="the step's cell sort: the counting sort by cell (the default) or the "
+                         "onesweep radix sort (same permutation); single, large and batch "
+                         "workloads and the plain one-by-one comparison")
     ap.add_argument("--first-pass", choices=["auto", "fused", "split"], default="auto",
                     help="single and large scenes: list build fused with the first lambda pass, "
                          "apart from it, or the tuner's (or default) choice")
