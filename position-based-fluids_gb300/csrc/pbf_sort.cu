@@ -412,9 +412,14 @@ inline uint32_t blocks_for(uint64_t n, uint32_t t) {
 // particles in registers and lists the larger ones, k_cell_fix_big sorts
 // those of up to kBigCell in shared memory (one CTA per cell) and larger
 // ones through a per-CTA bitmap of the particle indices.
-constexpr uint32_t kScanItems = 8;
-constexpr uint32_t kScanTile = kSortThreads * kScanItems;  // counts per scan tile
+constexpr uint32_t kScanItems = 8;                            // counts per thread and chunk
+constexpr uint32_t kScanChunk = kSortThreads * kScanItems;   // 2048
+constexpr uint32_t kScanChunks = 4;
+constexpr uint32_t kScanTile = kScanChunk * kScanChunks;     // counts per scan tile
 constexpr uint32_t kSmallCell = 16;
+// control words: [0] scan tiles started, [1] big cells, [2] huge cells,
+// [3] the operator's error word, [4] out-of-order small cells
+constexpr uint32_t kCtlHeader = 8;
 constexpr uint32_t kBigCell = 8192;
 
 // Exclusive prefix of tile `tile` from the look-back words of the tiles
@@ -456,33 +461,52 @@ __device__ __forceinline__ uint32_t warp_lookback(uint32_t *lookback, uint32_t t
 }
 
 // off[c] = particles in cells below c, for c in [0, ncells]; counts[c] -> 0.
-// Tiles of kScanTile counts are numbered in the order CTAs start.
+// Tiles of kScanTile counts (kScanChunks chunks of 2048, each thread holding
+// 8 consecutive counts of every chunk) are numbered in the order CTAs start.
 __global__ void __launch_bounds__(kSortThreads)
     k_count_scan(uint32_t *__restrict__ counts, uint32_t ncells, uint32_t total,
                  uint32_t *__restrict__ off, uint32_t *ctl, uint32_t *err) {
-  __shared__ uint32_t s_tile, s_total, s_excl;
+  __shared__ uint32_t s_tile, s_excl;
+  __shared__ uint32_t s_chunk[kScanChunks];
   __shared__ uint32_t s_warp[kSortWarps];
-  uint32_t *lookback = ctl + 4;
+  uint32_t *lookback = ctl + kCtlHeader;
   const uint32_t tid = threadIdx.x;
   if (tid == 0) s_tile = atomicAdd(&ctl[0], 1u);
   __syncthreads();
   const uint32_t tile = s_tile;
-  const uint32_t base = tile * kScanTile + tid * kScanItems;
-  uint32_t v[kScanItems], sum = 0;
+  uint32_t v[kScanChunks][kScanItems], texcl[kScanChunks];
 #pragma unroll
-  for (uint32_t j = 0; j < kScanItems; ++j) {
-    const uint32_t idx = base + j;
-    v[j] = idx < ncells ? counts[idx] : 0u;
-    sum += v[j];
+  for (uint32_t q = 0; q < kScanChunks; ++q) {
+    const uint32_t base = tile * kScanTile + q * kScanChunk + tid * kScanItems;
+    uint32_t sum = 0;
+    // two 16-byte loads where the counts are 16-byte aligned (base is a
+    // multiple of 8)
+    if (base + kScanItems <= ncells && (reinterpret_cast<uintptr_t>(counts + base) & 15u) == 0u) {
+      const uint4 a = *reinterpret_cast<const uint4 *>(counts + base);
+      const uint4 b = *reinterpret_cast<const uint4 *>(counts + base + 4);
+      v[q][0] = a.x; v[q][1] = a.y; v[q][2] = a.z; v[q][3] = a.w;
+      v[q][4] = b.x; v[q][5] = b.y; v[q][6] = b.z; v[q][7] = b.w;
+      if (a.x | a.y | a.z | a.w) *reinterpret_cast<uint4 *>(counts + base) = make_uint4(0, 0, 0, 0);
+      if (b.x | b.y | b.z | b.w)
+        *reinterpret_cast<uint4 *>(counts + base + 4) = make_uint4(0, 0, 0, 0);
+    } else {
+#pragma unroll
+      for (uint32_t j = 0; j < kScanItems; ++j) {
+        const uint32_t idx = base + j;
+        v[q][j] = idx < ncells ? counts[idx] : 0u;
+        if (v[q][j]) counts[idx] = 0u;
+      }
+    }
+#pragma unroll
+    for (uint32_t j = 0; j < kScanItems; ++j) sum += v[q][j];
+    texcl[q] = block_exclusive_scan(sum, s_warp);
+    if (tid == kSortThreads - 1) s_chunk[q] = texcl[q] + sum;
+    __syncthreads();
   }
-#pragma unroll
-  for (uint32_t j = 0; j < kScanItems; ++j)
-    if (v[j]) counts[base + j] = 0u;
-  const uint32_t texcl = block_exclusive_scan(sum, s_warp);
-  if (tid == kSortThreads - 1) s_total = texcl + sum;
-  __syncthreads();
   if (tid < 32) {
-    const uint32_t tot = s_total;
+    uint32_t tot = 0;
+#pragma unroll
+    for (uint32_t q = 0; q < kScanChunks; ++q) tot += s_chunk[q];
     if (tile == 0) {
       if (tid == 0) {
         st_volatile(&lookback[0], kLbInclusive | tot);
@@ -500,27 +524,26 @@ __global__ void __launch_bounds__(kSortThreads)
     }
   }
   __syncthreads();
-  uint32_t run = s_excl + texcl;
+  uint32_t carry = s_excl;
 #pragma unroll
-  for (uint32_t j = 0; j < kScanItems; ++j) {
-    const uint32_t idx = base + j;
-    if (idx < ncells) off[idx] = run;
-    run += v[j];
-  }
-}
-
-// The counting of the predict kernel, from a key array (the operator).
-// A key outside [0, ncells) is not counted and sets kDevErrKey in *err.
-__global__ void __launch_bounds__(256)
-    k_count_keys(const uint32_t *__restrict__ keys, uint32_t n, uint32_t ncells,
-                 uint32_t *__restrict__ counts, uint32_t *__restrict__ pos, uint32_t *err) {
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-    const uint32_t i = base + threadIdx.x;
-    const uint32_t key = i < n ? keys[i] : 0u;
-    const bool valid = i < n && key < ncells;
-    if (i < n && !valid) atomicOr(err, kDevErrKey);
-    count_cell_key(key, valid, i, counts, pos);
+  for (uint32_t q = 0; q < kScanChunks; ++q) {
+    const uint32_t base = tile * kScanTile + q * kScanChunk + tid * kScanItems;
+    uint32_t run = carry + texcl[q];
+    uint32_t o[kScanItems];
+#pragma unroll
+    for (uint32_t j = 0; j < kScanItems; ++j) {
+      o[j] = run;
+      run += v[q][j];
+    }
+    if (base + kScanItems <= ncells && (reinterpret_cast<uintptr_t>(off + base) & 15u) == 0u) {
+      *reinterpret_cast<uint4 *>(off + base) = make_uint4(o[0], o[1], o[2], o[3]);
+      *reinterpret_cast<uint4 *>(off + base + 4) = make_uint4(o[4], o[5], o[6], o[7]);
+    } else {
+#pragma unroll
+      for (uint32_t j = 0; j < kScanItems; ++j)
+        if (base + j < ncells) off[base + j] = o[j];
+    }
+    carry += s_chunk[q];
   }
 }
 
@@ -541,35 +564,28 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// One thread per cell: a cell of up to kSmallCell particles sorted by index
-// in registers (bitonic network, only when out of order); larger cells
-// listed for k_cell_fix_big.
+// The counting of the predict kernel, from a key array (the operator).
+// A key outside [0, ncells) is not counted and sets kDevErrKey in *err.
 __global__ void __launch_bounds__(256)
-    k_cell_fix(const uint32_t *__restrict__ off, uint32_t ncells, uint32_t *__restrict__ perm,
-               uint32_t *__restrict__ big, uint32_t big_cap, uint32_t *__restrict__ huge,
-               uint32_t huge_cap, uint32_t *ctl) {
-  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncells) return;
-  const uint32_t a = off[c], m = off[c + 1] - a;
-  if (m <= 1u) return;
-  if (m > kSmallCell) {
-    if (m <= kBigCell) {
-      const uint32_t q = atomicAdd(&ctl[1], 1u);
-      if (q < big_cap) big[q] = c;
-    } else {
-      const uint32_t q = atomicAdd(&ctl[2], 1u);
-      if (q < huge_cap) huge[q] = c;
-    }
-    return;
+    k_count_keys(const uint32_t *__restrict__ keys, uint32_t n, uint32_t ncells,
+                 uint32_t *__restrict__ counts, uint32_t *__restrict__ pos, uint32_t *err) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t key = i < n ? keys[i] : 0u;
+    const bool valid = i < n && key < ncells;
+    if (i < n && !valid) atomicOr(err, kDevErrKey);
+    count_cell_key(key, valid, i, counts, pos);
   }
+}
+
+// Cells of 2..kSmallCell particles put back in index order in registers
+// (bitonic network).
+__device__ __forceinline__ void sort_small_cell(uint32_t *__restrict__ perm, uint32_t a,
+                                                uint32_t m) {
   uint32_t v[kSmallCell];
-  bool sorted = true;
 #pragma unroll
-  for (uint32_t j = 0; j < kSmallCell; ++j) {
-    v[j] = j < m ? perm[a + j] : 0xffffffffu;
-    if (j > 0 && j < m && v[j] < v[j - 1]) sorted = false;
-  }
-  if (sorted) return;
+  for (uint32_t j = 0; j < kSmallCell; ++j) v[j] = j < m ? perm[a + j] : 0xffffffffu;
 #pragma unroll
   for (uint32_t k = 2; k <= kSmallCell; k <<= 1)
 #pragma unroll
@@ -590,6 +606,51 @@ __global__ void __launch_bounds__(256)
     if (j < m) perm[a + j] = v[j];
 }
 
+// One thread per cell.  A cell of 2..kSmallCell particles whose indices are
+// out of order (most are in order: their particles were counted by one warp)
+// is sorted here (kSortHere, on grids with at least two particles per cell)
+// or listed for k_cell_fix_big (sparse grids, where this kernel runs over
+// mostly empty cells and is kept light in registers); larger cells are
+// listed by size.
+template <bool kSortHere>
+__global__ void __launch_bounds__(256)
+    k_cell_fix(const uint32_t *__restrict__ off, uint32_t ncells, uint32_t *__restrict__ perm,
+               uint32_t *__restrict__ small, uint32_t small_cap, uint32_t *__restrict__ big,
+               uint32_t big_cap, uint32_t *__restrict__ huge, uint32_t huge_cap, uint32_t *ctl) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const uint32_t a = off[c], m = off[c + 1] - a;
+  if (m <= 1u) return;
+  if (m > kSmallCell) {
+    if (m <= kBigCell) {
+      const uint32_t q = atomicAdd(&ctl[1], 1u);
+      if (q < big_cap) big[q] = c;
+    } else {
+      const uint32_t q = atomicAdd(&ctl[2], 1u);
+      if (q < huge_cap) huge[q] = c;
+    }
+    return;
+  }
+  uint32_t prev = perm[a];
+  bool sorted = true;
+#pragma unroll 1
+  for (uint32_t j = 1; j < m; ++j) {
+    const uint32_t x = perm[a + j];
+    if (x < prev) {
+      sorted = false;
+      break;
+    }
+    prev = x;
+  }
+  if (sorted) return;
+  if (kSortHere) {
+    sort_small_cell(perm, a, m);
+  } else {
+    const uint32_t q = atomicAdd(&ctl[4], 1u);
+    if (q < small_cap) small[q] = c;
+  }
+}
+
 constexpr uint32_t kHugeCtas = 4;  // CTAs that take the huge cells (one bitmap each)
 
 // The listed cells: up to kBigCell particles sorted in shared memory (one
@@ -598,6 +659,7 @@ constexpr uint32_t kHugeCtas = 4;  // CTAs that take the huge cells (one bitmap 
 // then write the marked indices in ascending order.
 __global__ void __launch_bounds__(kSortThreads)
     k_cell_fix_big(const uint32_t *__restrict__ off, uint32_t *__restrict__ perm,
+                   const uint32_t *__restrict__ small, uint32_t small_cap,
                    const uint32_t *__restrict__ big, uint32_t big_cap,
                    const uint32_t *__restrict__ huge, uint32_t huge_cap, const uint32_t *ctl,
                    uint32_t *__restrict__ bitmap, uint32_t bm_words, uint32_t bm_stride) {
@@ -605,7 +667,14 @@ __global__ void __launch_bounds__(kSortThreads)
   __shared__ uint32_t s_warp[kSortWarps];
   __shared__ uint32_t s_total;
   const uint32_t tid = threadIdx.x;
+  const uint32_t nsmall = min(ctl[4], small_cap);
   const uint32_t nbig = min(ctl[1], big_cap), nhuge = min(ctl[2], huge_cap);
+  // the listed small cells: one thread each
+  for (uint32_t w = blockIdx.x * kSortThreads + tid; w < nsmall; w += gridDim.x * kSortThreads) {
+    const uint32_t c = small[w];
+    const uint32_t a = off[c];
+    sort_small_cell(perm, a, off[c + 1] - a);
+  }
   for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
     const uint32_t c = big[b];
     const uint32_t a = off[c], m = off[c + 1] - a;
@@ -790,6 +859,7 @@ CellSortPlan make_cell_sort_plan(uint32_t n, uint32_t ncells) {
   p.n = n;
   p.ncells = ncells;
   p.tiles = (uint32_t)(((uint64_t)ncells + kScanTile - 1) / kScanTile);
+  p.small_cap = (uint32_t)std::min<uint64_t>(ncells, (uint64_t)n / 2 + 1);
   p.big_cap = (uint32_t)std::min<uint64_t>(ncells, (uint64_t)n / (kSmallCell + 1) + 1);
   p.huge_cap = n / (kBigCell + 1) + 1;
   p.bm_words = (n + 31u) / 32u;
@@ -802,9 +872,11 @@ CellSortPlan make_cell_sort_plan(uint32_t n, uint32_t ncells) {
   w += n;
   w = (w + 63) & ~size_t(63);
   p.off_ctl = w;
-  p.ctl_words = 4 + (size_t)p.tiles;
+  p.ctl_words = kCtlHeader + (size_t)p.tiles;
   w += p.ctl_words;
   w = (w + 63) & ~size_t(63);
+  p.off_small = w;
+  w += p.small_cap;
   p.off_big = w;
   w += p.big_cap;
   p.off_huge = w;
@@ -821,7 +893,7 @@ CellSortPlan resize_cell_sort_plan(const CellSortPlan &cap, uint32_t n, uint32_t
   p.n = std::min(n, cap.n);
   p.ncells = std::min(ncells, cap.ncells);
   p.tiles = (uint32_t)(((uint64_t)p.ncells + kScanTile - 1) / kScanTile);
-  p.ctl_words = 4 + (size_t)p.tiles;
+  p.ctl_words = kCtlHeader + (size_t)p.tiles;
   p.bm_words = (p.n + 31u) / 32u;
   return p;
 }
@@ -849,14 +921,22 @@ cudaError_t cell_sort_finish(const CellSortPlan &plan, const uint32_t *keys, uin
       keys, scratch + plan.off_pos, offsets, plan.n, plan.ncells, skeys, perm);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_cell_fix<<<blocks_for(plan.ncells, 256), 256, 0, stream>>>(
-      offsets, plan.ncells, perm, scratch + plan.off_big, plan.big_cap, scratch + plan.off_huge,
-      plan.huge_cap, ctl);
+  // dense grids sort their small cells in the pass over the cells, sparse
+  // ones list them (measured: 1M particles in 64^3 cells, 14.6M in 14.6M)
+  if ((uint64_t)plan.ncells * 2u <= plan.n)
+    k_cell_fix<true><<<blocks_for(plan.ncells, 256), 256, 0, stream>>>(
+        offsets, plan.ncells, perm, scratch + plan.off_small, plan.small_cap,
+        scratch + plan.off_big, plan.big_cap, scratch + plan.off_huge, plan.huge_cap, ctl);
+  else
+    k_cell_fix<false><<<blocks_for(plan.ncells, 256), 256, 0, stream>>>(
+        offsets, plan.ncells, perm, scratch + plan.off_small, plan.small_cap,
+        scratch + plan.off_big, plan.big_cap, scratch + plan.off_huge, plan.huge_cap, ctl);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_cell_fix_big<<<kStrideCtas / 4u, kSortThreads, 0, stream>>>(
-      offsets, perm, scratch + plan.off_big, plan.big_cap, scratch + plan.off_huge,
-      plan.huge_cap, ctl, scratch + plan.off_bitmap, plan.bm_words, plan.bm_stride);
+      offsets, perm, scratch + plan.off_small, plan.small_cap, scratch + plan.off_big,
+      plan.big_cap, scratch + plan.off_huge, plan.huge_cap, ctl, scratch + plan.off_bitmap,
+      plan.bm_words, plan.bm_stride);
   return cudaGetLastError();
 }
 

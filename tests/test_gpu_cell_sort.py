@@ -78,6 +78,8 @@ CASES = [
     ("one_key", "uniform", 1, 3),
     ("one_cell_grid", "uniform", 5000, 1),
     ("ragged_tiles", "uniform", 4097, 2049),
+    ("ragged_scan_tiles", "uniform", 60_000, 3 * 8192 + 2049 + 5),
+    ("many_scan_tiles", "uniform", 1 << 20, 3_000_001),
 ]
 
 
