@@ -275,3 +275,25 @@ def test_oracle_scenes_match_the_library_generator(oracle_mod):
             if f != "pad_":
                 assert list(np.atleast_1d(getattr(a, f))) == list(np.atleast_1d(getattr(b, f))), \
                     (sc.name, f)
+
+
+def test_scorr_taken_in_units_of_h2(oracle_mod):
+    """s_corr = -k h^2 (W(r)/W(dq h))^n, the reading the paper equations use:
+    with k = 0.1 a resting 16^3 block settles (mean density within 2% of
+    rest, speeds below 1 m/s after 20 steps), while the literal k = 0.1 m^2
+    (k h^2 with k = 10 at h = 0.1) outweighs lambda and throws the block
+    apart within the same 20 steps."""
+    cfg, pos, vel = oracle_mod.dam_break_scene((16, 16, 16), (1.6, 1.6, 1.6))
+    prm = oracle_mod.benchmark_paper_params(cfg)
+    prm.gravity_y = 0.0  # at rest: only the constraint and s_corr act
+    out, ovel, dens, *_ = oracle_mod.paper_steps_f64(prm, pos, vel, 20, threads=0)
+    assert np.isfinite(out).all()
+    assert np.abs(ovel[:, :3]).max() < 1.0
+    interior = dens > 0.8 * prm.rest_density
+    assert abs(dens[interior].mean() / prm.rest_density - 1.0) < 0.02
+    literal = oracle_mod.benchmark_paper_params(cfg)
+    literal.gravity_y = 0.0
+    literal.scorr_k = 0.1 / (literal.h * literal.h)
+    out2, ovel2, *_ = oracle_mod.paper_steps_f64(literal, pos, vel, 20, threads=0)
+    speed2 = np.abs(ovel2[:, :3]).max() if np.isfinite(ovel2).all() else np.inf
+    assert speed2 > 50.0, speed2
