@@ -30,7 +30,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [*ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-I", str(REPO / "include")]
 # Translation units whose arithmetic must not be contracted into FMAs.
-NO_FMAD = {"pbf_refcompat.cu"}
+NO_FMAD = {"pbf_refcompat.cu", "pbf_render.cu"}
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
              "-Wno-unused-parameter", "-I", str(CUDA_HOME / "include"), "-I", str(REPO / "include")]
 
@@ -64,7 +64,8 @@ def _compile_jobs(force: bool, extra_nvcc: list[str]) -> tuple[list[list[str]], 
         src = SRC / name
         obj = OBJ / (name + ".o")
         objs.append(obj)
-        flags = NVCC_FLAGS + (["-fmad=false"] if name in NO_FMAD else []) + extra_nvcc
+        flags = NVCC_FLAGS + (["-fmad=false", "-Xcompiler", "-ffp-contract=off"]
+                              if name in NO_FMAD else []) + extra_nvcc
         if force or _stale(obj, [src, *common_deps]):
             jobs.append([NVCC, *flags, "-c", str(src), "-o", str(obj)])
     for name in CPP_SOURCES:

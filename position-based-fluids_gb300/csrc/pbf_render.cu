@@ -12,6 +12,12 @@
 // clamp(dot(n, (1,1,1)), 0, 1)); depth test GL_LESS with depth cleared to 1
 // and colour cleared to 0.05 grey.
 //
+// The translation unit is compiled with -fmad=false (and its host code
+// without floating-point contraction): every expression rounds operator by
+// operator in IEEE binary32, with correctly rounded division and square
+// root, so the image is reproducible bit for bit by a restatement that
+// evaluates the same expressions in the same order.
+//
 // GL rasterises points in submission order; here each pixel keeps the
 // fragment of least depth, ties to the lowest input index (the particle GL
 // would have drawn first), through a 64-bit atomicMin on (depth bits, index),
@@ -114,7 +120,7 @@ __global__ void k_render_shade(const float4 *__restrict__ X, const uint32_t *__r
       point_coord(x, y, s, ix, iy, mx, my);
       const float l2 = mx * mx + my * my;
       const float nz = sqrtf(fmaxf(0.0f, 1.0f - l2));
-      const float inv = rsqrtf(fmaxf(l2 + nz * nz, 1e-30f));
+      const float inv = 1.0f / sqrtf(fmaxf(l2 + nz * nz, 1e-30f));
       const float cosang = fminf(fmaxf((mx + my + nz) * inv, 0.0f), 1.0f);
       r = p.w * cosang;
       g = p.w * cosang;
