@@ -185,7 +185,7 @@ uint32_t sort_pass_launches(const SortPlan &plan);
 // Layout of its scratch (32-bit words):
 struct CellSortPlan {
   uint32_t n = 0, ncells = 0, tiles = 0;
-  uint32_t small_cap = 0, big_cap = 0, huge_cap = 0;
+  uint32_t small_cap = 0, med_cap = 0, big_cap = 0, huge_cap = 0;
   uint32_t bm_words = 0;   // words of a bitmap over the n particle indices
   uint32_t bm_stride = 0;  // words from one CTA's bitmap to the next
   size_t off_counts = 0;  // ncells: per-cell counts (zero between steps)
@@ -193,7 +193,8 @@ struct CellSortPlan {
   size_t off_ctl = 0;     // 8 control words (list counts, an error word), then the
   size_t ctl_words = 0;   //     scan's look-back words (zeroed before every step)
   size_t off_small = 0;   // cells of 2..16 particles out of index order
-  size_t off_big = 0;     // cells of 17..8192 particles
+  size_t off_med = 0;     // cells of 17..64 particles
+  size_t off_big = 0;     // cells of 65..8192 particles
   size_t off_huge = 0;    // cells of more than 8192
   size_t off_bitmap = 0;  // one bitmap of the particle indices per huge-cell CTA
   size_t words = 0;

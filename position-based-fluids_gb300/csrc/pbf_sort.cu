@@ -417,8 +417,10 @@ constexpr uint32_t kScanChunk = kSortThreads * kScanItems;   // 2048
 constexpr uint32_t kScanChunks = 4;
 constexpr uint32_t kScanTile = kScanChunk * kScanChunks;     // counts per scan tile
 constexpr uint32_t kSmallCell = 16;
+constexpr uint32_t kWarpCell = 64;  // cells of 17..64 particles: one warp each
 // control words: [0] scan tiles started, [1] big cells, [2] huge cells,
-// [3] the operator's error word, [4] out-of-order small cells
+// [3] the operator's error word, [4] out-of-order small cells, [5] cells
+// for one warp
 constexpr uint32_t kCtlHeader = 8;
 constexpr uint32_t kBigCell = 8192;
 
@@ -615,14 +617,18 @@ __device__ __forceinline__ void sort_small_cell(uint32_t *__restrict__ perm, uin
 template <bool kSortHere>
 __global__ void __launch_bounds__(256)
     k_cell_fix(const uint32_t *__restrict__ off, uint32_t ncells, uint32_t *__restrict__ perm,
-               uint32_t *__restrict__ small, uint32_t small_cap, uint32_t *__restrict__ big,
-               uint32_t big_cap, uint32_t *__restrict__ huge, uint32_t huge_cap, uint32_t *ctl) {
+               uint32_t *__restrict__ small, uint32_t small_cap, uint32_t *__restrict__ med,
+               uint32_t med_cap, uint32_t *__restrict__ big, uint32_t big_cap,
+               uint32_t *__restrict__ huge, uint32_t huge_cap, uint32_t *ctl) {
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   const uint32_t a = off[c], m = off[c + 1] - a;
   if (m <= 1u) return;
   if (m > kSmallCell) {
-    if (m <= kBigCell) {
+    if (m <= kWarpCell) {
+      const uint32_t q = atomicAdd(&ctl[5], 1u);
+      if (q < med_cap) med[q] = c;
+    } else if (m <= kBigCell) {
       const uint32_t q = atomicAdd(&ctl[1], 1u);
       if (q < big_cap) big[q] = c;
     } else {
@@ -651,6 +657,36 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// A cell of up to 64 particles put back in index order by one warp: lane l
+// holds entries l and l + 32, bitonic network across the warp.
+__device__ __forceinline__ void warp_sort_cell(uint32_t *__restrict__ perm, uint32_t a,
+                                               uint32_t m) {
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t v[2];
+  v[0] = lane < m ? perm[a + lane] : 0xffffffffu;
+  v[1] = lane + 32u < m ? perm[a + lane + 32u] : 0xffffffffu;
+#pragma unroll
+  for (uint32_t k = 2; k <= 64; k <<= 1)
+#pragma unroll
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      if (j == 32) {  // entries lane and lane + 32, in this thread
+        const uint32_t lo = min(v[0], v[1]), hi = max(v[0], v[1]);
+        v[0] = lo;  // k = 64: ascending for every entry below 64
+        v[1] = hi;
+      } else {
+#pragma unroll
+        for (uint32_t h = 0; h < 2; ++h) {
+          const uint32_t i = lane + 32u * h;
+          const uint32_t y = __shfl_xor_sync(0xffffffffu, v[h], (int)j);
+          const bool keep_min = ((i & j) == 0u) == ((i & k) == 0u);
+          v[h] = keep_min ? min(v[h], y) : max(v[h], y);
+        }
+      }
+    }
+  if (lane < m) perm[a + lane] = v[0];
+  if (lane + 32u < m) perm[a + lane + 32u] = v[1];
+}
+
 constexpr uint32_t kHugeCtas = 4;  // CTAs that take the huge cells (one bitmap each)
 
 // The listed cells: up to kBigCell particles sorted in shared memory (one
@@ -660,6 +696,7 @@ constexpr uint32_t kHugeCtas = 4;  // CTAs that take the huge cells (one bitmap 
 __global__ void __launch_bounds__(kSortThreads)
     k_cell_fix_big(const uint32_t *__restrict__ off, uint32_t *__restrict__ perm,
                    const uint32_t *__restrict__ small, uint32_t small_cap,
+                   const uint32_t *__restrict__ med, uint32_t med_cap,
                    const uint32_t *__restrict__ big, uint32_t big_cap,
                    const uint32_t *__restrict__ huge, uint32_t huge_cap, const uint32_t *ctl,
                    uint32_t *__restrict__ bitmap, uint32_t bm_words, uint32_t bm_stride) {
@@ -674,6 +711,14 @@ __global__ void __launch_bounds__(kSortThreads)
     const uint32_t c = small[w];
     const uint32_t a = off[c];
     sort_small_cell(perm, a, off[c + 1] - a);
+  }
+  // cells of 17..64: one warp each
+  const uint32_t nmed = min(ctl[5], med_cap);
+  for (uint32_t w = (blockIdx.x * kSortThreads + tid) >> 5; w < nmed;
+       w += gridDim.x * kSortWarps) {
+    const uint32_t c = med[w];
+    const uint32_t a = off[c];
+    warp_sort_cell(perm, a, off[c + 1] - a);
   }
   for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
     const uint32_t c = big[b];
@@ -860,7 +905,8 @@ CellSortPlan make_cell_sort_plan(uint32_t n, uint32_t ncells) {
   p.ncells = ncells;
   p.tiles = (uint32_t)(((uint64_t)ncells + kScanTile - 1) / kScanTile);
   p.small_cap = (uint32_t)std::min<uint64_t>(ncells, (uint64_t)n / 2 + 1);
-  p.big_cap = (uint32_t)std::min<uint64_t>(ncells, (uint64_t)n / (kSmallCell + 1) + 1);
+  p.med_cap = (uint32_t)std::min<uint64_t>(ncells, (uint64_t)n / (kSmallCell + 1) + 1);
+  p.big_cap = (uint32_t)std::min<uint64_t>(ncells, (uint64_t)n / (kWarpCell + 1) + 1);
   p.huge_cap = n / (kBigCell + 1) + 1;
   p.bm_words = (n + 31u) / 32u;
   p.bm_stride = p.bm_words;
@@ -877,6 +923,8 @@ CellSortPlan make_cell_sort_plan(uint32_t n, uint32_t ncells) {
   w = (w + 63) & ~size_t(63);
   p.off_small = w;
   w += p.small_cap;
+  p.off_med = w;
+  w += p.med_cap;
   p.off_big = w;
   w += p.big_cap;
   p.off_huge = w;
@@ -926,17 +974,19 @@ cudaError_t cell_sort_finish(const CellSortPlan &plan, const uint32_t *keys, uin
   if ((uint64_t)plan.ncells * 2u <= plan.n)
     k_cell_fix<true><<<blocks_for(plan.ncells, 256), 256, 0, stream>>>(
         offsets, plan.ncells, perm, scratch + plan.off_small, plan.small_cap,
-        scratch + plan.off_big, plan.big_cap, scratch + plan.off_huge, plan.huge_cap, ctl);
+        scratch + plan.off_med, plan.med_cap, scratch + plan.off_big, plan.big_cap,
+        scratch + plan.off_huge, plan.huge_cap, ctl);
   else
     k_cell_fix<false><<<blocks_for(plan.ncells, 256), 256, 0, stream>>>(
         offsets, plan.ncells, perm, scratch + plan.off_small, plan.small_cap,
-        scratch + plan.off_big, plan.big_cap, scratch + plan.off_huge, plan.huge_cap, ctl);
+        scratch + plan.off_med, plan.med_cap, scratch + plan.off_big, plan.big_cap,
+        scratch + plan.off_huge, plan.huge_cap, ctl);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_cell_fix_big<<<kStrideCtas / 4u, kSortThreads, 0, stream>>>(
-      offsets, perm, scratch + plan.off_small, plan.small_cap, scratch + plan.off_big,
-      plan.big_cap, scratch + plan.off_huge, plan.huge_cap, ctl, scratch + plan.off_bitmap,
-      plan.bm_words, plan.bm_stride);
+      offsets, perm, scratch + plan.off_small, plan.small_cap, scratch + plan.off_med,
+      plan.med_cap, scratch + plan.off_big, plan.big_cap, scratch + plan.off_huge, plan.huge_cap,
+      ctl, scratch + plan.off_bitmap, plan.bm_words, plan.bm_stride);
   return cudaGetLastError();
 }
 

@@ -1,9 +1,9 @@
 """The counting sort of cell keys (the PAPER step's sort, pbf_op_sort_cells):
 the stable permutation and the CSR cell offsets, bit-exact against numpy's
 stable argsort and against the onesweep radix sort, for every path a cell
-can take -- up to 16 keys (sorted in registers), 17..8192 (shared memory),
-more (a bitmap of the indices) -- and the whole step with either sort giving
-the same bits."""
+can take -- up to 16 keys (sorted by one thread), 17..64 (one warp),
+65..8192 (shared memory), more (a bitmap of the indices) -- and the whole
+step with either sort giving the same bits."""
 from __future__ import annotations
 
 import zlib
@@ -74,6 +74,8 @@ CASES = [
     ("descending", "descending", 300_001, 5000),
     ("one_cell_huge", "one_cell", 100_000, 7),
     ("big_cells", "big_cells", 200_000, 50),
+    ("warp_cells", "uniform", 300_000, 10_000),      # ~30 per cell: one warp each
+    ("around_64", "uniform", 640_000, 10_000),       # either side of 64 per cell
     ("mixed", "mixed", 400_000, 100_000),
     ("one_key", "uniform", 1, 3),
     ("one_cell_grid", "uniform", 5000, 1),
