@@ -470,8 +470,9 @@ size_t pbf_op_sort_cells_scratch_bytes(uint32_t n, uint32_t ncells);
  * pbf_op_sort_pairs with values NULL followed by pbf_op_cell_offsets.
  * Keys are counted per cell with warp-aggregated atomics, the counts
  * scanned into the offsets (decoupled look-back), every key scattered to its
- * cell, and each cell put back in index order (in registers up to 16 keys,
- * in shared memory up to 8192, through a bitmap of the indices beyond).
+ * cell, and each cell put back in index order (by one thread up to 16 keys,
+ * one warp up to 64, in shared memory up to 8192, through a bitmap of the
+ * indices beyond).
  * Outputs must not alias the keys.  No reference counterpart beyond the
  * intent of init_cells.cl + find_cells.cl + the radix kernels. */
 int pbf_op_sort_cells(const uint32_t *d_keys, uint32_t n, uint32_t ncells,
