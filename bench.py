@@ -547,10 +547,13 @@ def run_ours(args) -> int:
     if args.load_state:
         sim.load_state(args.load_state)
     tuning = None if args.no_tune else sim.autotune(3).as_dict()
-    if args.first_pass != "auto" or args.staged != "auto" or args.sort != "auto":
+    if (args.first_pass != "auto" or args.staged != "auto" or args.sort != "auto"
+            or args.build != "auto"):
         t = sim.tuning()
         if args.first_pass != "auto":
             t.fuse_first = 1 if args.first_pass == "fused" else 0
+        if args.build != "auto":
+            t.masked_build = 1 if args.build == "masked" else 0
         if args.staged != "auto":
             t.staged = 1 if args.staged == "on" else 0
         if args.sort != "auto":
@@ -1107,6 +1110,10 @@ def main() -> int:
     ap.add_argument("--first-pass", choices=["auto", "fused", "split"], default="auto",
                     help="single and large scenes: list build fused with the first lambda pass, "
                          "apart from it, or the tuner's (or default) choice")
+    ap.add_argument("--build", choices=["auto", "masked", "scan"], default="auto",
+                    help="single and large scenes: the list build testing each row into a "
+                         "membership mask before storing members, storing members as they are "
+                         "found, or the tuner's (or default) choice (same lists)")
     ap.add_argument("--forms", choices=["all", "none"], default="all",
                     help="single workload: also run the batched and served workloads and "
                          "summarise them in the line (one GPU only)")

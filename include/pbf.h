@@ -232,8 +232,10 @@ int pbf_launches_per_step(const pbf_sim *sim, uint32_t *launches);
  * asynchronous copies and read neighbours from there (threads, batch and
  * fuse_first then do not apply).  radix_sort = 1 sorts the step's cell keys
  * with the onesweep radix sort instead of the counting sort by cell (the
- * default); both give the stable permutation.  No choice changes a result
- * bit.  trial_ms is the tuner's best time per launch of each pass (0 when
+ * default); both give the stable permutation.  masked_build = 1 (the
+ * default) has the list build (0 and 1) test each row of candidates into a
+ * membership mask and store the members from the mask afterwards; 0 stores
+ * each member as it is found.  No choice changes a result bit.  trial_ms is the tuner's best time per launch of each pass (0 when
  * untuned). */
 typedef struct pbf_tuning {
   uint32_t threads[6];
@@ -242,6 +244,7 @@ typedef struct pbf_tuning {
   float trial_ms[6];
   uint32_t staged;
   uint32_t radix_sort;
+  uint32_t masked_build;
 } pbf_tuning;
 /* Times every shape over `trial_steps` steps (1..32) of this simulation
  * from its current state, keeps the fastest per pass and restores the state

@@ -114,12 +114,13 @@ class Tuning(C.Structure):
 
     PASSES = ("nbr_build", "nbr_lambda", "lambda", "delta", "vorticity", "xsph_commit")
     _fields_ = [("threads", C.c_uint32 * 6), ("batch", C.c_uint32 * 6), ("fuse_first", C.c_uint32),
-                ("trial_ms", C.c_float * 6), ("staged", C.c_uint32), ("radix_sort", C.c_uint32)]
+                ("trial_ms", C.c_float * 6), ("staged", C.c_uint32), ("radix_sort", C.c_uint32),
+                ("masked_build", C.c_uint32)]
 
     def as_dict(self) -> dict:
         return {"threads": dict(zip(self.PASSES, self.threads)), "batch": dict(zip(self.PASSES, self.batch)),
                 "fuse_first": int(self.fuse_first), "staged": int(self.staged),
-                "radix_sort": int(self.radix_sort),
+                "radix_sort": int(self.radix_sort), "masked_build": int(self.masked_build),
                 "trial_ms": dict(zip(self.PASSES, self.trial_ms))}
 
 

@@ -246,6 +246,10 @@ struct GatherTuning {
   // 1: the onesweep radix sort of the cell keys instead of the counting
   // sort by cell (same permutation)
   uint8_t radix_sort = 0;
+  // 1: the list build tests each row's candidates into a membership mask and
+  // stores the members from it afterwards (same lists; 3% faster build, 6%
+  // faster fused build on the 1M-particle dam break)
+  uint8_t masked_build = 1;
 };
 constexpr int kBlockCodes = 3;  // 64, 128, 256
 constexpr int kBatchCodes = 2;  // 4, 8

@@ -142,8 +142,10 @@ __global__ void __launch_bounds__(256)
 // Neighbour-list build from the predicted positions P (which equal the
 // step-start positions the fallback recomputes).  Each member's slot is
 // stored straight into its list word; the rest of the last word holds the
-// particle's own slot.
-template <int kBlock>
+// particle's own slot.  kMasked: the candidates of each row are tested into
+// a membership mask first and the members stored from it afterwards
+// (scan_members_masked); the same lists either way.
+template <int kBlock, bool kMasked>
 __global__ void __launch_bounds__(kBlock)
     k_nbr_build(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
                 uint4 *__restrict__ nbr4, uint32_t *__restrict__ nbr_cnt) {
@@ -153,11 +155,15 @@ __global__ void __launch_bounds__(kBlock)
   uint32_t *__restrict__ out = reinterpret_cast<uint32_t *>(nbr4) + 4ull * k;
   const size_t stride = 4ull * c.n;  // words from one list group to the next
   uint32_t cnt = 0;
-  scan_members(pk, nc.skeys[k], scene_of(nc.scenes, nc.sid, k), nc.off, P, c,
-               [&](uint32_t j, const Sep &) {
-                 if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j;
-                 ++cnt;
-               });
+  const auto store = [&](uint32_t j) {
+    if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j;
+    ++cnt;
+  };
+  const SceneDesc &sc = scene_of(nc.scenes, nc.sid, k);
+  if constexpr (kMasked)
+    scan_members_masked(pk, nc.skeys[k], sc, nc.off, P, c, store);
+  else
+    scan_members(pk, nc.skeys[k], sc, nc.off, P, c, [&](uint32_t j, const Sep &) { store(j); });
   pad_list(out, stride, cnt, c.maxn, k);
   nbr_cnt[k] = cnt;
   record_count(nc.cnt_max, cnt);
@@ -167,8 +173,10 @@ __global__ void __launch_bounds__(kBlock)
 // summed over the members in the order the lists store them -- the bits
 // k_lambda computes from the lists.  (In one kernel a warp executes the
 // lambda arithmetic whenever any of its lanes has a member, so which form is
-// faster depends on the scene; the tuner picks.)
-template <int kBlock>
+// faster depends on the scene; the tuner picks.)  kMasked: the members come
+// from row masks (scan_members_masked) and each member's separation is
+// evaluated again from its position, the same operations on the same values.
+template <int kBlock, bool kMasked>
 __global__ void __launch_bounds__(kBlock)
     k_nbr_lambda(const float4 *__restrict__ P, NbrCtx nc, PaperConsts c,
                  uint4 *__restrict__ nbr4, uint32_t *__restrict__ nbr_cnt,
@@ -180,12 +188,21 @@ __global__ void __launch_bounds__(kBlock)
   const size_t stride = 4ull * c.n;  // words from one list group to the next
   uint32_t cnt = 0;
   LambdaAcc acc{c.w_self, 0.f, 0.f, 0.f, 0.f};
-  scan_members(pk, nc.skeys[k], scene_of(nc.scenes, nc.sid, k), nc.off, P, c,
-               [&](uint32_t j, const Sep &r) {
-                 if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j;
-                 ++cnt;
-                 acc.add(r, c);
-               });
+  const auto store = [&](uint32_t j) {
+    if (cnt < c.maxn) out[(size_t)(cnt >> 2) * stride + (cnt & 3u)] = j;
+    ++cnt;
+  };
+  const SceneDesc &sc = scene_of(nc.scenes, nc.sid, k);
+  if constexpr (kMasked)
+    scan_members_masked(pk, nc.skeys[k], sc, nc.off, P, c, [&](uint32_t j) {
+      store(j);
+      acc.add(separation(pk, __ldg(&P[j])), c);
+    });
+  else
+    scan_members(pk, nc.skeys[k], sc, nc.off, P, c, [&](uint32_t j, const Sep &r) {
+      store(j);
+      acc.add(r, c);
+    });
   pad_list(out, stride, cnt, c.maxn, k);
   nbr_cnt[k] = cnt;
   record_count(nc.cnt_max, cnt);
@@ -391,10 +408,13 @@ cudaError_t paper_reorder(const uint32_t *perm, const float4 *X,
 #define PBF_BUILD_LAUNCH(KERNEL, KIND, ...)                                           \
   do {                                                                                 \
     const int slot_ = d.timer ? d.timer->begin(KIND, st) : -1;                         \
-    switch (d.tune.block[KIND]) {                                                      \
-      case 0: KERNEL<64><<<blocks_for(c.n, 64), 64, 0, st>>>(__VA_ARGS__); break;       \
-      case 1: KERNEL<128><<<blocks_for(c.n, 128), 128, 0, st>>>(__VA_ARGS__); break;    \
-      case 2: KERNEL<256><<<blocks_for(c.n, 256), 256, 0, st>>>(__VA_ARGS__); break;    \
+    switch (d.tune.block[KIND] * 2 + (d.tune.masked_build ? 1 : 0)) {                  \
+      case 0: KERNEL<64, false><<<blocks_for(c.n, 64), 64, 0, st>>>(__VA_ARGS__); break;    \
+      case 1: KERNEL<64, true><<<blocks_for(c.n, 64), 64, 0, st>>>(__VA_ARGS__); break;     \
+      case 2: KERNEL<128, false><<<blocks_for(c.n, 128), 128, 0, st>>>(__VA_ARGS__); break; \
+      case 3: KERNEL<128, true><<<blocks_for(c.n, 128), 128, 0, st>>>(__VA_ARGS__); break;  \
+      case 4: KERNEL<256, false><<<blocks_for(c.n, 256), 256, 0, st>>>(__VA_ARGS__); break; \
+      case 5: KERNEL<256, true><<<blocks_for(c.n, 256), 256, 0, st>>>(__VA_ARGS__); break;  \
       default: return cudaErrorInvalidValue;                                           \
     }                                                                                  \
     if (d.timer) d.timer->end(slot_, st);                                              \

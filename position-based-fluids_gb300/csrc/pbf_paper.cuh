@@ -339,6 +339,69 @@ __device__ __forceinline__ void scan_members(const float4 &pk, uint32_t key, con
   }
 }
 
+// scan_members with the member work taken out of the candidate loop: each
+// row is tested 32 candidates at a time into a membership mask (bit e for
+// candidate c0 + e), then member(j) runs for the mask's set bits in
+// ascending order -- the same members in the same order as scan_members.
+// Lanes of a warp test candidates of different cells, so in scan_members
+// the member branch runs for nearly every candidate (some lane of the warp
+// has a member); here the candidate loop is the load, the distance and one
+// bit in every lane, and the member work runs as many times per chunk as
+// the warp's largest member count in it.
+template <typename F>
+__device__ __forceinline__ void scan_members_masked(const float4 &pk, uint32_t key,
+                                                    const SceneDesc &s,
+                                                    const uint32_t *__restrict__ off,
+                                                    const float4 *__restrict__ P,
+                                                    const PaperConsts &c, F &&member) {
+  const int nx = s.ncell[0], ny = s.ncell[1], nz = s.ncell[2];
+  const uint32_t local = key - s.cell_base;
+  const int cx = (int)(local % (uint32_t)nx);
+  const uint32_t t = local / (uint32_t)nx;
+  const int cy = (int)(t % (uint32_t)ny);
+  const int cz = (int)(t / (uint32_t)ny);
+  const int x0 = cx > 0 ? cx - 1 : 0;
+  const int x1 = cx + 1 < nx ? cx + 1 : nx - 1;
+  for (int dz = -1; dz <= 1; ++dz) {
+    const int z = cz + dz;
+    if (z < 0 || z >= nz) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = cy + dy;
+      if (y < 0 || y >= ny) continue;
+      const uint32_t row = s.cell_base + (uint32_t)nx * ((uint32_t)y + (uint32_t)ny * (uint32_t)z);
+      const uint32_t a = __ldg(&off[row + x0]);
+      const uint32_t b = __ldg(&off[row + x1 + 1]);
+      for (uint32_t c0 = a; c0 < b; c0 += 32u) {
+        const uint32_t c1 = min(c0 + 32u, b);
+        uint32_t m = 0, bit = 1u;
+        uint32_t j = c0;
+        for (; j + 4u <= c1; j += 4, bit <<= 4) {
+          const float4 *__restrict__ q = P + j;
+          float4 d[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) d[e] = __ldg(q + e);
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (is_pair(separation(pk, d[e]).r2, c.h2)) m |= bit << e;
+        }
+        if (j < c1) {
+          float4 d[3];
+#pragma unroll
+          for (int e = 0; e < 3; ++e) d[e] = __ldg(&P[min(j + e, c1 - 1u)]);
+#pragma unroll
+          for (int e = 0; e < 3; ++e)
+            if (j + e < c1 && is_pair(separation(pk, d[e]).r2, c.h2)) m |= bit << e;
+        }
+        while (m) {
+          const uint32_t e = (uint32_t)__ffs(m) - 1u;
+          m &= m - 1u;
+          member(c0 + e);
+        }
+      }
+    }
+  }
+}
+
 // Fills the rest of a listed set's last word with the particle's own slot
 // (maxn is a multiple of 8, so the word is inside the list capacity).
 __device__ __forceinline__ void pad_list(uint32_t *__restrict__ out, size_t stride,

@@ -241,6 +241,7 @@ void to_pbf_tuning(const GatherTuning &g, const double trial_ms[kGatherKinds], p
   out->fuse_first = g.fuse_first;
   out->staged = g.staged;
   out->radix_sort = g.radix_sort;
+  out->masked_build = g.masked_build;
 }
 
 int to_gather_tuning(const pbf_tuning &t, GatherTuning *out) {
@@ -273,6 +274,11 @@ int to_gather_tuning(const pbf_tuning &t, GatherTuning *out) {
     return PBF_ERR_INVALID;
   }
   g.radix_sort = (uint8_t)t.radix_sort;
+  if (t.masked_build > 1) {
+    set_error_message("tuning: masked_build must be 0 or 1");
+    return PBF_ERR_INVALID;
+  }
+  g.masked_build = (uint8_t)t.masked_build;
   *out = g;
   return PBF_OK;
 }

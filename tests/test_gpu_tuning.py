@@ -2,8 +2,9 @@
 
 Statement (checked below): every launch shape -- 64/128/256 threads per CTA,
 4 or 8 neighbour loads in flight, list build fused with the first lambda or
-not -- gives BIT-IDENTICAL steps, and pbf_autotune leaves the simulation's
-state unchanged, so a tuned run is bitwise the untuned run.
+not, members stored as found or from row masks -- gives BIT-IDENTICAL
+steps, and pbf_autotune leaves the simulation's state unchanged, so a tuned
+run is bitwise the untuned run.
 """
 from __future__ import annotations
 
@@ -19,12 +20,13 @@ def bits(a):
     return np.ascontiguousarray(a, np.float32).view(np.uint32)
 
 
-def shape(pbf, threads, batch, fuse):
+def shape(pbf, threads, batch, fuse, masked=0):
     t = pbf.Tuning()
     for k in range(6):
         t.threads[k] = threads
         t.batch[k] = batch
     t.fuse_first = fuse
+    t.masked_build = masked
     return t
 
 
@@ -53,10 +55,11 @@ def test_every_launch_shape_gives_the_same_bits(pbf):
     for prm in (sc.params, small):
         scene = pbf.scenes.Scene(sc.name, prm, sc.particles, 8)
         ref, launches = run(pbf, scene, 8)
-        for threads, batch, fuse in itertools.product((64, 128, 256), (4, 8), (0, 1)):
-            got, n = run(pbf, scene, 8, shape(pbf, threads, batch, fuse))
+        for threads, batch, fuse, masked in itertools.product((64, 128, 256), (4, 8), (0, 1),
+                                                              (0, 1)):
+            got, n = run(pbf, scene, 8, shape(pbf, threads, batch, fuse, masked))
             for g, r in zip(got, ref):
-                assert np.array_equal(bits(g), bits(r)), (threads, batch, fuse)
+                assert np.array_equal(bits(g), bits(r)), (threads, batch, fuse, masked)
             assert n == launches - fuse
 
 
@@ -79,7 +82,8 @@ def test_invalid_shapes_are_rejected(pbf):
     sc = pbf.scenes.dam_break((6, 6, 6), (0.8, 0.8, 0.8), seed=33)
     with pbf.Simulation(sc.params, sc.particles) as sim:
         sim.init()
-        for bad in (shape(pbf, 96, 4, 0), shape(pbf, 128, 6, 0), shape(pbf, 128, 4, 2)):
+        for bad in (shape(pbf, 96, 4, 0), shape(pbf, 128, 6, 0), shape(pbf, 128, 4, 2),
+                    shape(pbf, 128, 4, 0, 2)):
             with pytest.raises(pbf.PbfError) as ex:
                 sim.set_tuning(bad)
             assert ex.value.status == pbf.ERR_INVALID
