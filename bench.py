@@ -713,15 +713,19 @@ def with_sort(obj, sort: str):
     return obj
 
 
-def plain_one_by_one(pbf, scenes, steps: int, sample_steps: int, ext_stream_of, sort: str = "auto"):
+def plain_one_by_one(pbf, scenes, steps, sample_steps: int, ext_stream_of, sort: str = "auto"):
     """The scenes solved one at a time on the plain path: per scene, create,
-    upload, warm up, then time `sample_steps` graph-replayed steps with CUDA
-    events.  Returns per-scene seconds for `steps` steps (sampled rate x
-    steps) and the wall seconds of set-up plus read-back per scene."""
+    upload, warm up (3 steps), then time its steps as graph-replayed steps
+    with CUDA events -- all of them (`sample_steps` 0), or the first
+    `sample_steps` scaled to the scene's count.  `steps` is one count for
+    every scene or one per scene.  Returns per-scene seconds for its steps and
+    the wall seconds of set-up plus read-back per scene."""
     import torch
 
     step_s, setup_s = [], []
-    for s in scenes:
+    for i, s in enumerate(scenes):
+        n_steps = steps[i] if isinstance(steps, (list, tuple)) else steps
+        timed = n_steps if sample_steps <= 0 else max(1, min(sample_steps, n_steps))
         w0 = time.perf_counter()
         sim = pbf.Simulation(s.params, s.particles)
         sim.init()
@@ -731,11 +735,11 @@ def plain_one_by_one(pbf, scenes, steps: int, sample_steps: int, ext_stream_of, 
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(ext)
-        sim.step(sample_steps, sync=False)
+        sim.step(timed, sync=False)
         e1.record(ext)
         e1.synchronize()
         sim.sync()
-        t = e0.elapsed_time(e1) / 1e3 / sample_steps * steps
+        t = e0.elapsed_time(e1) / 1e3 / timed * n_steps
         sim.dumpData()
         sim.close()
         step_s.append(t)
@@ -800,7 +804,7 @@ def run_batch(args, emit: bool = True):
     # ---- the same scenes one by one on the plain path ---------------------
     plain = None
     if rank == 0 and not args.no_plain:
-        sample = max(3, min(steps, args.plain_sample))
+        sample = args.plain_sample
         plain_step_s, plain_setup_s = plain_one_by_one(
             pbf, scenes, steps, sample, lambda sim: torch.cuda.ExternalStream(sim.stream()),
             args.sort)
@@ -811,8 +815,9 @@ def run_batch(args, emit: bool = True):
                  "scene_latency_s": {"p50": float(np.percentile(done, 50)),
                                      "p99": float(np.percentile(done, 99))},
                  "method": f"each scene alone through the plain C-ABI path (CUDA-graph steps); "
-                           f"{sample} timed steps per scene after 3 warm-up steps, scaled to {steps}; "
-                           f"latency = completion time of scene k when solved in sequence"}
+                           + (f"all {steps} steps of each scene timed after 3 warm-up steps; " if sample <= 0
+                              else f"{sample} timed steps per scene after 3 warm-up steps, scaled to {steps}; ")
+                           + f"latency = completion time of scene k when solved in sequence"}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
@@ -913,15 +918,17 @@ def run_serve(args, emit: bool = True):
     if not args.no_plain:
         sample = args.plain_sample
         plain_step_s, plain_setup_s = plain_one_by_one(
-            pbf, (r.scene() for r in reqs), 1, sample, lambda sim: torch.cuda.ExternalStream(sim.stream()))
-        service = [ps * r.steps + su for ps, su, r in zip(plain_step_s, plain_setup_s, reqs)]
+            pbf, [r.scene() for r in reqs], [r.steps for r in reqs], sample,
+            lambda sim: torch.cuda.ExternalStream(sim.stream()))
+        service = [ps + su for ps, su in zip(plain_step_s, plain_setup_s)]
         plat, pend = fifo_latencies([r.arrival for r in reqs], service)
         plain = {"value": total_work / (pend - reqs[0].arrival), "unit": UNIT,
                  "scene_latency_s": {"p50": float(np.percentile(plat, 50)),
                                      "p99": float(np.percentile(plat, 99))},
                  "method": f"each request alone through the plain C-ABI path: measured set-up and read-back, "
-                           f"{sample} CUDA-event-timed graph steps after 3 warm-up steps scaled to its step "
-                           f"count; latencies from these service times in arrival order (one at a time)"}
+                           f"{'all its' if sample <= 0 else sample} CUDA-event-timed graph steps after 3 "
+                           f"warm-up steps{'' if sample <= 0 else ' scaled to its step count'}; latencies "
+                           f"from these service times in arrival order (one at a time)"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": int(st["batch_steps"]),
         "warmup": 1, "ms_per_step": makespan / max(1, st["batch_steps"]) * 1e3, "higher_is_better": True,
@@ -1096,8 +1103,9 @@ def main() -> int:
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-fp64", action="store_true",
                     help="skip the one-step comparison with the FP64 oracle after the timed steps")
-    ap.add_argument("--plain-sample", type=int, default=30,
-                    help="timed steps per scene of the one-by-one plain comparison")
+    ap.add_argument("--plain-sample", type=int, default=0,
+                    help="timed steps per scene of the one-by-one plain comparison, scaled to the "
+                         "scene's step count (0, the default: every step of every scene)")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-by-one plain comparison")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--staged", choices=["auto", "on", "off"], default="auto",

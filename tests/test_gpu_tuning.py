@@ -44,7 +44,7 @@ def run(pbf, sc, steps, tuning=None, autotune=0):
                 assert np.array_equal(bits(x), bits(y)), "autotune changed the state"
             steps -= 2
         sim.step(steps)
-        return sim.dumpData(), sim.launches_per_step()
+        return sim.dumpData(), (sim.launches_per_step(), sim.tuning().fuse_first)
 
 
 def test_every_launch_shape_gives_the_same_bits(pbf):
@@ -54,13 +54,13 @@ def test_every_launch_shape_gives_the_same_bits(pbf):
     small.grow_lists = 0
     for prm in (sc.params, small):
         scene = pbf.scenes.Scene(sc.name, prm, sc.particles, 8)
-        ref, launches = run(pbf, scene, 8)
+        ref, (launches, default_fuse) = run(pbf, scene, 8)
         for threads, batch, fuse, masked in itertools.product((64, 128, 256), (4, 8), (0, 1),
                                                               (0, 1)):
-            got, n = run(pbf, scene, 8, shape(pbf, threads, batch, fuse, masked))
+            got, (n, _) = run(pbf, scene, 8, shape(pbf, threads, batch, fuse, masked))
             for g, r in zip(got, ref):
                 assert np.array_equal(bits(g), bits(r)), (threads, batch, fuse, masked)
-            assert n == launches - fuse
+            assert n == launches + default_fuse - fuse  # fused: one launch fewer
 
 
 def test_autotune_keeps_state_and_results(pbf):
