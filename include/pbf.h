@@ -225,8 +225,8 @@ int pbf_launches_per_step(const pbf_sim *sim, uint32_t *launches);
  * neighbour-list build, 1 the list build fused with the first lambda, 2
  * lambda, 3 delta-p, 4 vorticity, 5 XSPH + commit.  threads = 64, 128 or
  * 256 per CTA; batch = 4 or 8 neighbour loads in flight per thread (ignored
- * for 0 and 1); fuse_first = 1 runs 1 instead of 0 + 2 for the first solver
- * iteration.  staged = 1 runs every gather pass on staged cell blocks
+ * for 0 and 1); fuse_first = 1 (the default) runs 1 instead of 0 + 2 for
+ * the first solver iteration.  staged = 1 runs every gather pass on staged cell blocks
  * instead: persistent CTAs walk the step's occupied blocks of 4 x 4 x 4
  * cells, copy each block's neighbourhood into shared memory with bulk
  * asynchronous copies and read neighbours from there (threads, batch and
