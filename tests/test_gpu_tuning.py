@@ -106,3 +106,29 @@ def test_batch_autotune_keeps_results(pbf):
     for a, c in zip(*out):
         for x, y in zip(a, c):
             assert np.array_equal(bits(x), bits(y))
+
+
+def test_masked_build_with_rows_over_32_candidates(pbf):
+    """A block at twice the linear density (spacing h/4: ~64 particles per
+    cell, rows of ~190 candidates) makes the masked list build test each row
+    in several 32-candidate chunks; fused or not, it gives the lists and
+    bits of the build that stores members as it finds them."""
+    box, cells = (0.8, 0.8, 0.8), (8, 8, 8)
+    p = pbf.scenes.base_params(box, cells)
+    p.max_neighbours = 512
+    m = 0.25 * pbf.scenes.H
+    ps = pbf.generate_block((m, m, m), 16, 16, 16, 0.025, 0.01 * 0.025, pbf.scenes.MASS, 77)
+    scene = pbf.scenes.Scene("dense_block", p, ps, 3)
+    for fuse in (0, 1):
+        out = []
+        for masked in (0, 1):
+            with pbf.Simulation(scene.params, scene.particles) as sim:
+                sim.init()
+                sim.set_tuning(shape(pbf, 128, 4, fuse, masked))
+                sim.step(1)
+                mx, over = sim.neighbour_stats()
+                assert mx > 128 and over == 0, (mx, over)
+                sim.step(2)
+                out.append(sim.dumpData())
+        for a, b in zip(*out):
+            assert np.array_equal(bits(a), bits(b)), fuse
