@@ -752,6 +752,28 @@ def plain_one_by_one(pbf, scenes, steps, sample_steps: int, ext_stream_of, sort:
     return step_s, setup_s
 
 
+def plain_by_size(sizes, plain_step_s, steps: int, t_batch: float) -> list:
+    """The plain one-by-one time by scene size: per bucket of particle
+    counts, the scenes, their share of the particles, their share of the
+    plain time, their plain rate and the ratio the batch would show on them
+    alone at its whole-mix rate per particle."""
+    sizes = np.asarray(sizes)
+    secs = np.asarray(plain_step_s)
+    total_n, total_t = sizes.sum(), secs.sum()
+    out = []
+    for lo, hi in ((0, 32768), (32768, 131072), (131072, 1 << 31)):
+        sel = (sizes >= lo) & (sizes < hi)
+        if not sel.any():
+            continue
+        n, t = int(sizes[sel].sum()), float(secs[sel].sum())
+        rate = n * ITERATIONS * steps / t
+        out.append({"particles": [lo, min(hi, int(sizes.max()))], "scenes": int(sel.sum()),
+                    "particle_share": float(n / total_n), "plain_time_share": float(t / total_t),
+                    "plain_value": float(rate),
+                    "batch_over_plain": float((total_n * ITERATIONS * steps / t_batch) / rate)})
+    return out
+
+
 def run_batch(args, emit: bool = True):
     """256 independent dam-break scenes of log-uniform sizes advanced together
     (one launch per kernel per step, CUDA-graph step) against the same scenes
@@ -819,6 +841,7 @@ def run_batch(args, emit: bool = True):
                  "seconds_device": t_plain,
                  "scene_latency_s": {"p50": float(np.percentile(done, 50)),
                                      "p99": float(np.percentile(done, 99))},
+                 "by_scene_size": plain_by_size([s.n for s in scenes], plain_step_s, steps, t_dev),
                  "method": f"each scene alone through the plain C-ABI path (CUDA-graph steps); "
                            + (f"all {steps} steps of each scene timed after 3 warm-up steps; " if sample <= 0
                               else f"{sample} timed steps per scene after 3 warm-up steps, scaled to {steps}; ")
@@ -977,6 +1000,8 @@ def form_summaries(args) -> dict:
             "particles": b["config"]["particles"], "steps": b["steps"], "value": b["value"],
             "unit": b["unit"], "ms_per_step": b["ms_per_step"], "e2e": b["e2e"]["value"],
             "plain_one_by_one": b["plain_one_by_one"]["value"] if b["plain_one_by_one"] else None,
+            "plain_by_scene_size": (b["plain_one_by_one"]["by_scene_size"]
+                                    if b["plain_one_by_one"] else None),
             "speedup_vs_plain": b["speedup_vs_plain"], "scene_latency_s": b["scene_latency_s"]["p50"],
             "gpu_launches": b["gpu_launches"], "clocks": b["clocks"]}
     def served_summary(s):
